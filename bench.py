@@ -1,0 +1,371 @@
+"""Benchmark: Chebyshev (KPM) density of states at scale on one GB300.
+
+Workload (one "step" = one full DoS solve): honeycomb lattice, 2 sites per
+cell, nearest-neighbour t = -2.7, Anderson on-site disorder U[-0.5, 0.5]
+(seed 1), 1024 x 1024 cells periodic (2,097,152 sites, 6.29M hoppings),
+rescale bounds +-8.7 (|E| <= 3|t| + 0.5), M = 2048 Chebyshev moments, R = 32
+random-phase vectors (e^{i theta}, seed 0), complex64 recursion with FP64
+moment sums and Chebyshev doubling (bras = kets), Jackson kernel, rho(E) on
+4096 energies reconstructed in FP64 on the device.
+
+metric: site-moment-vector updates/s = N * M * R / step time.
+  value : inputs resident in HBM (H~ and the kets block), device-timed.
+  e2e   : the same solve through the C ABI drop-in (tbk_cheb_braket_real) with
+          pinned HOST buffers: H~ CSC + kets uploaded and moments read back
+          inside the timed region.
+Also measured in the same run: the plain FP64 GPU path (complex128, one
+moment per step, bras read every step — the reference's algorithm, fused) and
+the CPU oracle (the reference's CPU recursion restated in C, OpenMP over the
+random vectors) on a bounded sample.
+
+--impl reference: times the CPU restatement of the reference's KPM loop
+(TB/numerical.h:363-381) on all host cores, on a bounded sample of the same
+workload (the reference itself cannot be built: Eigen/FFTW/Spectra/C++23 are
+absent), and prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Chebyshev site-moment-vector updates/s vs FP64 plain; p50/p99 solve latency"
+UNIT = "site-moment-vector updates/s"
+L_CELLS = 1024
+T_HOP = -2.7
+W_DIS = 1.0            # U[-W/2, W/2] = U[-0.5, 0.5]
+BOUND = 8.7
+M_MOM = 2048
+R_VEC = 32
+N_E = 4096
+WORKLOAD = ("KPM DoS: honeycomb 1024x1024 periodic (2,097,152 sites, nnz(H) 6.29M + 2.10M diag), "
+            "t=-2.7, disorder U[-0.5,0.5] seed 1, M=2048, R=32 random-phase vectors seed 0, "
+            "complex64 recursion + FP64 moments (doubling), Jackson kernel, rho(E) on 4096 energies")
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(cp, ri, v, n, steps, threads):
+    """Oracle recursion (plain path: one moment per step) on a bounded sample."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+
+    kets = orc.random_phase_kets(n, R_VEC, 0)
+    t0 = time.perf_counter()
+    orc.cheb_moments(n, cp, ri, v, steps + 1, kets, kets, threads=threads, steps_limit=steps)
+    dt = time.perf_counter() - t0
+    return n * R_VEC * steps / dt, dt
+
+
+def build_host_system():
+    """The rescaled H~ of the workload as host CSC arrays (built on the device)."""
+    import tight_binding_gb300 as tb
+
+    X = tb.PartialLattice(tb.Honeycomb().add_hopping("A", 1, T_HOP), (L_CELLS, L_CELLS))
+    X.set_scalar_disorder(W_DIS, 1)
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], float)
+    G = tb.GreenFunction(M_MOM, H, -BOUND, BOUND)
+    return X, H, G
+
+
+def oracle_system():
+    """Same H~ built by the CPU oracle (reference arm: no GPU involved)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+
+    s3 = np.sqrt(3.0)
+    bases = np.array([[1.5, -s3 / 2, 0], [1.5, s3 / 2, 0]]).T
+    pos = np.array([[0, 0, 0], [1, 0, 0.0]])
+    # canonical table of Honeycomb + add_hopping("A", 1NN, t) + set_scalar_field zeros
+    hf = [1, 1, 1, 0, 1]
+    ht = [0, 0, 0, 0, 1]
+    hv = [[1, 0, 0], [0, 1, 0], [0, 0, 0], [0, 0, 0], [0, 0, 0]]
+    tt = [T_HOP, T_HOP, T_HOP, 0.0, 0.0]
+    N = 2 * L_CELLS * L_CELLS
+    V = orc.uniform_disorder(N, W_DIS, 1)
+    spec = orc.LatticeSpec(2, [L_CELLS, L_CELLS], bases, pos, hf, ht, hv, tt, mode=orc.MODE_PERIODIC_BARE,
+                           is_complex=False, extend=[1, 1], scalar_site=V)
+    cp, ri, v = orc.build_csc(spec)
+    ocp, ori, ov = orc.rescale_csc(N, cp, ri, v, BOUND, 0.0)
+    return N, ocp, ori, ov
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    N, cp, ri, v = oracle_system()
+    steps_per_sample = args.cpu_steps
+    if args.warmup > 0:
+        cpu_sample(cp, ri, v, N, 1, threads)
+    vals, times = [], []
+    for _ in range(args.steps):
+        r, dt = cpu_sample(cp, ri, v, N, steps_per_sample, threads)
+        vals.append(r)
+        times.append(dt)
+    value = float(np.mean(vals))
+    sample = (f"{steps_per_sample} recursion steps (one moment each) of the workload's H~ x 32 vectors per "
+              f"step, C restatement of TB/numerical.h:363-381, OpenMP over vectors")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sites": N, "moments": M_MOM, "vectors": R_VEC},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    import tight_binding_gb300 as tb
+    from tight_binding_gb300 import capi
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    X, H, G = build_host_system()
+    Ht = G.scaled_HE
+    N = Ht.shape[0]
+    # resident inputs: kets block (Eigen layout N x R column-major complex128)
+    kets_h = tb.bases_of_uniform_ampl_with_random_phases(N, R_VEC, 0 + rank)
+    kets_d = torch.from_numpy(np.ascontiguousarray(kets_h.T)).to(dev)        # (R, N) row-major == N x R col-major
+    mu_d = torch.zeros(M_MOM, dtype=torch.float64, device=dev)
+    solver = tb.KpmSolver(Ht, R_VEC, precision="mixed", doubling=True, flags=capi.FLAG_DEVICE_PTRS)
+    E = np.cos((np.arange(N_E) + 0.5) * np.pi / N_E) * 0.999
+    jack = tb.Jackson()
+
+    def step():
+        with torch.cuda.stream(stream):
+            solver.run_device(M_MOM, kets_d.data_ptr(), kets_d.data_ptr(), mu_d.data_ptr(), sh)
+            mu = mu_d.cpu().numpy()
+        rho = tb.dos_from_moments(mu, jack, R_VEC, E)
+        return mu, rho
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    rec_ms, rec_launch, rec_bytes = [], 0, 0.0
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for k in range(args.steps):
+        mu, rho = step()
+        ev[k + 1].record(stream)
+        ms, nl, b = solver.last_timing()
+        rec_ms.append(ms)
+        rec_launch, rec_bytes = nl, b
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    updates = float(N) * M_MOM * R_VEC
+    value = ws * updates * args.steps / (total_ms / 1e3)
+
+    if rank != 0:
+        if ws > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return 0
+
+    # ---- roofline of the recursion kernel (live CUDA events on the launching stream)
+    peak, peak_kind = peaks()
+    avg_launch_ms = float(np.mean(rec_ms)) / rec_launch
+    achieved = rec_bytes / (avg_launch_ms / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "kpm_step_traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel": "kpm_step_kernel<float,32,real,doubling>", "launches_per_step": rec_launch,
+                "algorithmic_bytes_per_launch": rec_bytes, "avg_launch_us": avg_launch_ms * 1e3}
+
+    # ---- e2e through the C-ABI drop-in with pinned host buffers
+    cp, ri, v = Ht.to_csc()
+    cp_p = torch.from_numpy(cp).pin_memory()
+    ri_p = torch.from_numpy(ri).pin_memory()
+    v_p = torch.from_numpy(v).pin_memory()
+    kets_p = torch.from_numpy(np.ascontiguousarray(kets_h.T)).pin_memory()
+    mu_h = torch.zeros(M_MOM, dtype=torch.float64).pin_memory()
+    h2d = cp_p.numel() * 4 + ri_p.numel() * 4 + v_p.numel() * 8 + kets_p.numel() * 16
+    d2h = M_MOM * 8
+    flags = capi.PREC_MIXED | capi.FLAG_DOUBLING
+
+    def e2e_call():
+        kp = kets_p.data_ptr()
+        capi.check(capi.lib().tbk_cheb_braket_real(N, ri_p.numel(), cp_p.data_ptr(), ri_p.data_ptr(), v_p.data_ptr(),
+                                                  M_MOM, kp, kp, R_VEC, flags, mu_h.data_ptr()))
+
+    e2e_call()
+    e2e_steps = max(2, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_call()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": updates / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+           "ms_per_step": e2e_s * 1e3, "api": "tbk_cheb_braket_real (drop-in for cuda::Cheb_first_kind_seq_braket)"}
+    e2e_err = float(np.max(np.abs(mu_h.numpy() - mu)) / abs(mu[0]))
+
+    # ---- plain FP64 GPU path (reference algorithm, fused): one moment per step, bras read each step
+    fp = tb.KpmSolver(Ht, R_VEC, precision="fp64", doubling=False, flags=capi.FLAG_DEVICE_PTRS)
+    m64 = args.fp64_moments
+    mu64_d = torch.zeros(m64, dtype=torch.float64, device=dev)
+    with torch.cuda.stream(stream):
+        fp.run_device(m64, kets_d.data_ptr(), kets_d.data_ptr(), mu64_d.data_ptr(), sh)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    with torch.cuda.stream(stream):
+        fp.run_device(m64, kets_d.data_ptr(), kets_d.data_ptr(), mu64_d.data_ptr(), sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp_ms = e0.elapsed_time(e1)
+    fp_value = float(N) * m64 * R_VEC / (fp_ms / 1e3)
+    mu64 = mu64_d.cpu().numpy()
+    mixed_vs_fp64 = float(np.max(np.abs(mu[:m64] - mu64)) / abs(mu64[0]))
+    ms64, nl64, b64 = fp.last_timing()
+
+    # ---- CPU baseline: oracle on a bounded sample (all host cores)
+    threads = os.cpu_count() or 1
+    cpu_val, cpu_dt = cpu_sample(cp, ri, v, N, args.cpu_steps, threads)
+    cpu = {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{args.cpu_steps} recursion steps x 32 vectors of the same H~ ({cpu_dt:.1f} s), "
+                     f"C restatement of TB/numerical.h:363-381, OpenMP over vectors"}
+
+    launches_per_step = 1 + rec_launch + 2 + 2     # load kets, recursion, reduce+assemble, kernel+rho
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sites": int(N), "nnz_Ht": int(Ht.nnz), "moments": M_MOM,
+                   "vectors": R_VEC, "energies": N_E, "precision": "complex64 recursion, FP64 moment sums, doubling",
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (537 MB vector block per step, 129 MB L2); no flush"},
+        "latency_ms": {"p50": float(np.percentile(per_step, 50)), "p99": float(np.percentile(per_step, 99))},
+        "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
+        "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+        "fp64_plain": {"value": fp_value, "unit": UNIT, "moments": m64, "ms": fp_ms,
+                       "kernel_ms": ms64, "launches": nl64, "bytes_per_launch": b64,
+                       "speedup_mixed_over_fp64": value / fp_value},
+        "parity": {"mixed_vs_fp64_rel_err_first_%d_moments" % m64: mixed_vs_fp64, "e2e_vs_resident_rel": e2e_err},
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=64)
+    ap.add_argument("--fp64-moments", type=int, default=256)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

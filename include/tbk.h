@@ -1,0 +1,220 @@
+/*
+ * tbk.h — C ABI of the GB300 (sm_103a) kernel-polynomial library for
+ * chenzehan/tight_binding.
+ *
+ * Plain C: pointers, sizes and int status codes; no CUDA or C++ types in the
+ * signatures (streams are passed as `void*` holding a cudaStream_t; NULL is the
+ * legacy default stream).  Every entry point returns TBK_OK (0) or an error
+ * code, and tbk_last_error() gives the message of the calling thread's last
+ * failure.  There is no CPU fallback: without a usable GPU the compute entry
+ * points fail with TBK_ERR_CUDA.
+ *
+ * Layout conventions (those of the reference, which uses Eigen):
+ *   - complex numbers are interleaved (re, im) doubles (std::complex<double>);
+ *   - a block of R vectors is an N x R column-major complex matrix, ld = N
+ *     (Eigen::MatrixXcd), element (i, r) at [2*(r*N + i)];
+ *   - sparse matrices are compressed CSC with int32 indices, inner (row)
+ *     indices sorted within each column (Eigen::SparseMatrix<Scalar>,
+ *     outerIndexPtr / innerIndexPtr / valuePtr).
+ *
+ * Each declaration names the reference interface it replaces (file:line, paths
+ * relative to the reference project root).
+ */
+#ifndef TBK_H
+#define TBK_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  TBK_OK = 0,
+  TBK_ERR_INVALID = 1,      /* bad argument (the reference printed to cerr)      */
+  TBK_ERR_CUDA = 2,         /* CUDA runtime error / no device                    */
+  TBK_ERR_NOMEM = 3,        /* device allocation failed                          */
+  TBK_ERR_UNSUPPORTED = 4,  /* valid request outside what is implemented        */
+  TBK_ERR_TIMEOUT = 5,      /* bounded device wait gave up                       */
+  TBK_ERR_BUDGET = 6        /* request exceeds the admission (HBM) budget        */
+};
+const char* tbk_last_error(void);
+int tbk_version(void);
+/* Number of CUDA devices visible (0 without a GPU); never fails. */
+int tbk_device_count(void);
+
+/* ------------------------------------------------------------ precision */
+enum {
+  TBK_PREC_FP64 = 0,        /* complex128 recursion, FP64 H: the plain drop-in   */
+  TBK_PREC_MIXED = 1        /* complex64 recursion, FP32 H, FP64 moment sums     */
+};
+enum {
+  TBK_FLAG_PREC_MASK = 0xF,
+  TBK_FLAG_DOUBLING = 1 << 4,     /* bras == kets: mu_2n, mu_2n+1 from <v_n|v_n>,
+                                     <v_n+1|v_n> — half the recursion steps      */
+  TBK_FLAG_DEVICE_PTRS = 1 << 5,  /* bras/kets/mu are device pointers           */
+  TBK_FLAG_NO_L2_ZIGZAG = 1 << 6  /* keep every step's sweep ascending          */
+};
+
+/* =========================================================================
+ * Unit cell (host model).  Replaces UnitCell<Dim> construction and hopping
+ * management, TB/unit_cell.h:69-71, 188-256, 527-547, 678-707.
+ * ========================================================================= */
+typedef struct tbk_cell_s* tbk_cell;
+
+/* UnitCell(lattice_vectors, atoms), TB/unit_cell.h:188-210.
+ * lattice_vectors: dim rows of 3 doubles; positions: n_atoms rows of 3. */
+int tbk_cell_create(tbk_cell* out, int32_t dim, const double* lattice_vectors,
+                    int32_t n_atoms, const char* const* names, const double* positions);
+int tbk_cell_copy(tbk_cell* out, tbk_cell src);
+void tbk_cell_destroy(tbk_cell cell);
+/* add_hopping(from, to, lattice_vector, t), TB/unit_cell.h:212-228 (+534-547). */
+int tbk_cell_add_hopping(tbk_cell cell, const char* from, const char* to,
+                         const int32_t* lattice_vector, double t_re, double t_im);
+/* add_hopping(from, n_NN, t), TB/unit_cell.h:230-256; nn = 0 is On_Site. */
+int tbk_cell_add_hopping_nn(tbk_cell cell, const char* from, int32_t nn, double t_re,
+                            double t_im);
+/* get_atom_index, TB/unit_cell.h:101. */
+int tbk_cell_atom_index(tbk_cell cell, const char* name, int32_t* index);
+int tbk_cell_info(tbk_cell cell, int32_t* dim, int32_t* n_atoms, int32_t* n_hops);
+/* Canonical hopping table (from >= to), in enumeration order. */
+int tbk_cell_get_hoppings(tbk_cell cell, int32_t* from, int32_t* to, int32_t* latv3,
+                          double* t2);
+/* bases: 3 x dim column-major (Eigen bases); positions: n_atoms x 3. */
+int tbk_cell_get_geometry(tbk_cell cell, double* bases, double* positions);
+/* Number of warnings the last call produced (the reference's cerr messages,
+ * e.g. "Hopping already exists", TB/unit_cell.h:536-543). */
+int tbk_cell_last_warnings(tbk_cell cell, int32_t* count);
+
+/* =========================================================================
+ * Lattice and device Hamiltonian builder.  Replaces PartialLattice<Dim>,
+ * TB/lattice.h:22-117, 216-305, 313-377, 446-505.
+ * ========================================================================= */
+typedef struct tbk_lattice_s* tbk_lattice;
+
+/* PartialLattice(cell, span_size), TB/lattice.h:105-117. */
+int tbk_lattice_create(tbk_lattice* out, tbk_cell cell, const int32_t* span);
+void tbk_lattice_destroy(tbk_lattice lat);
+/* get_total_number, TB/lattice.h:51. */
+int tbk_lattice_total_number(tbk_lattice lat, int64_t* n);
+/* gauge_field, TB/lattice.h:73: A(r) = G r + c evaluated on the device (covers
+ * every uniform field in a linear gauge, e.g. Landau A = (0, B x, 0)). */
+int tbk_lattice_set_gauge_linear(tbk_lattice lat, const double* G_rowmajor_3x3,
+                                 const double* c3);
+/* gauge_field given by its value at every bare site (N x 3, host), for an
+ * arbitrary A(r) evaluated by the caller at atom_position(from, i_v). */
+int tbk_lattice_set_gauge_sites(tbk_lattice lat, const double* A_sites);
+int tbk_lattice_clear_gauge(tbk_lattice lat);
+/* set_scalar_field(f), TB/lattice.h:495-505, with f sampled at every bare site
+ * (N doubles, host).  Adds zero on-site hoppings to the cell as the reference does. */
+int tbk_lattice_set_scalar_sites(tbk_lattice lat, const double* V_sites);
+/* set_scalar_field with Anderson disorder V = W (u - 1/2), u ~ U[0,1) keyed by
+ * (seed, bare site index); generated on the device. */
+int tbk_lattice_set_scalar_disorder(tbk_lattice lat, double W, uint64_t seed);
+/* remove_atoms(atom, cells), TB/lattice.h:389-402: bare site flags (N, 1 = removed). */
+int tbk_lattice_set_removed(tbk_lattice lat, const uint8_t* removed_sites);
+/* index_comp construction, TB/lattice.h:446-457: number of kept sites. */
+int tbk_lattice_kept_number(tbk_lattice lat, int64_t* n);
+
+/* Device-resident sparse matrix (CSC + sliced-ELL). */
+typedef struct tbk_sparse_s* tbk_sparse;
+
+enum {
+  TBK_BUILD_SPARSE = 0,          /* get_Hamiltonian_sparse<Scalar>(), TB/lattice.h:262-305 */
+  TBK_BUILD_PERIODIC_BARE = 1,   /* get_Hamiltonian_periodic_extend_bare_sparse, :216-258 */
+  TBK_BUILD_BARE = 2             /* get_Hamiltonian_bare_sparse<Scalar>(), :347-377       */
+};
+/* Builds H on the device, bit-exact in structure with the reference's triplet
+ * list + setFromTriplets.  extend: per-axis periodic flags (PERIODIC_BARE only). */
+int tbk_build_hamiltonian(tbk_sparse* out, tbk_lattice lat, int32_t mode,
+                          const int32_t* extend, int32_t is_complex, void* stream);
+/* op_position(axis), TB/lattice.h:313-336: the diagonal X as a sparse matrix. */
+int tbk_build_position(tbk_sparse* out, tbk_lattice lat, int32_t axis, void* stream);
+/* Wraps a CSC (Eigen compressed layout).  device_ptrs: arrays already on the GPU. */
+int tbk_sparse_from_csc(tbk_sparse* out, int32_t rows, int32_t cols, int64_t nnz,
+                        const int32_t* col_ptr, const int32_t* row_idx,
+                        const double* values, int32_t is_complex, int32_t device_ptrs,
+                        void* stream);
+int tbk_sparse_info(tbk_sparse A, int32_t* rows, int32_t* cols, int64_t* nnz,
+                    int32_t* is_complex);
+/* Copies the CSC arrays to host buffers. */
+int tbk_sparse_download(tbk_sparse A, int32_t* col_ptr, int32_t* row_idx, double* values,
+                        void* stream);
+void tbk_sparse_destroy(tbk_sparse A);
+/* GreenFunction rescale (H - b I)/a, FP64 on the device; pattern = pattern(H)
+ * union diagonal as Eigen's sparse difference gives, TB/lattice.h:550-559. */
+int tbk_sparse_rescale(tbk_sparse* out, tbk_sparse H, double a, double b, void* stream);
+/* Velocity: v = X H - H X with X = op_position(axis) (values x_i h - h x_j,
+ * same pattern as H), TB/lattice.h:338-345 and TB/snippets.h:316-317. */
+int tbk_sparse_commutator(tbk_sparse* out, tbk_sparse H, tbk_sparse X, void* stream);
+
+/* =========================================================================
+ * Chebyshev (KPM) moments.
+ * ========================================================================= */
+/* Drop-in for cuda::Cheb_first_kind_seq_braket, real M overload,
+ * TB/numerics_cuda.cuh:10-11 / TB/numerics_cuda.cu:190-255: host CSC (square,
+ * compressed), bras/kets N x R column-major complex128; mu_out[k] =
+ * Re tr(bras^dagger T_k(M) kets), k < n.  n < 2 -> TBK_ERR_INVALID (the
+ * reference returns an empty vector).  flags: TBK_PREC_* | TBK_FLAG_DOUBLING
+ * (doubling needs bras == kets, same pointer). */
+int tbk_cheb_braket_real(int32_t n_rows, int64_t nnz, const int32_t* col_ptr,
+                         const int32_t* row_idx, const double* values, int32_t n,
+                         const double* bras, const double* kets, int32_t R, int32_t flags,
+                         double* mu_out);
+/* Complex M overload, TB/numerics_cuda.cuh:12-13 / TB/numerics_cuda.cu:266-323. */
+int tbk_cheb_braket_complex(int32_t n_rows, int64_t nnz, const int32_t* col_ptr,
+                            const int32_t* row_idx, const double* values, int32_t n,
+                            const double* bras, const double* kets, int32_t R,
+                            int32_t flags, double* mu_out);
+
+/* Resident solver: H~ and the recursion state stay on the device between runs.
+ * Replaces the per-call upload/alloc of TB/numerics_cuda.cu:199-222. */
+typedef struct tbk_kpm_s* tbk_kpm;
+int tbk_kpm_create(tbk_kpm* out, tbk_sparse Ht, int32_t R, int32_t flags);
+/* mu_out (host unless TBK_FLAG_DEVICE_PTRS in the plan's flags). */
+int tbk_kpm_run(tbk_kpm plan, int32_t n_mom, const double* bras, const double* kets,
+                double* mu_out, void* stream);
+/* DoS moments with device-generated random-phase kets (bras = kets),
+ * TB/numerical.h:120-122 + TB/functions.h:22-23; seed keys (seed, vector, site). */
+int tbk_kpm_run_random(tbk_kpm plan, int32_t n_mom, uint64_t seed, double* mu_out,
+                       void* stream);
+/* Device time of the recursion kernels of the last run (CUDA events on the
+ * launching stream), number of recursion launches and algorithmic DRAM bytes
+ * per launch. */
+int tbk_kpm_last_timing(tbk_kpm plan, double* ms_recursion, int32_t* launches,
+                        double* bytes_per_launch);
+void tbk_kpm_destroy(tbk_kpm plan);
+
+/* Random-phase kets exp(2 pi i u)/sqrt(N) (N x R column-major complex128, host),
+ * the seeded replacement of bases_of_uniform_ampl_with_random_phases,
+ * TB/numerical.h:120-122.  Host function (no GPU needed). */
+int tbk_random_phase_kets(int32_t n, int32_t R, uint64_t seed, double* kets);
+
+/* =========================================================================
+ * Kernels and reconstruction (FP64 on the device).
+ * ========================================================================= */
+enum { TBK_KERNEL_DIRICHLET = 0, TBK_KERNEL_FEJER = 1, TBK_KERNEL_LORENTZ = 2,
+       TBK_KERNEL_JACKSON = 3, TBK_KERNEL_LANCZOS = 4, TBK_KERNEL_WANG_ZUNGER = 5 };
+/* kernel_seq(N, kernel), TB/numerical.h:393-447.  p0/p1: lambda (Lorentz),
+ * M (Lanczos), alpha/beta (Wang-Zunger).  g_out: N doubles, host. */
+int tbk_kernel_seq(int32_t kind, int32_t N, double p0, double p1, double* g_out);
+/* GreenFunctionImag::operator()(z) = sum_n g_n Im(alpha_n(z)) mu_n for each z,
+ * TB/lattice.h:618-624 with TB/numerical.h:304-316.  z: 2*n_z doubles. */
+int tbk_green_imag_eval(int32_t n, const double* g, const double* mu, int32_t n_z,
+                        const double* z, double* out, void* stream);
+/* GreenFunctionImag::fft(upsample): DCT-III of g*mu at x_k = cos((k+1/2)pi/N')
+ * times 1/sqrt(1-x^2), N' = n*upsample (moments past n are zero),
+ * TB/lattice.h:625-640.  E_out, val_out: N' doubles. */
+int tbk_green_imag_fft(int32_t n, const double* g, const double* mu, int32_t upsample,
+                       double* E_out, double* val_out, void* stream);
+/* density_of_states_seq's last stage, TB/functions.h:26-30: rho(e) =
+ * -f(e)/(R pi) on a list of (already rescaled) energies. */
+int tbk_dos_from_moments(int32_t n, const double* mu, int32_t kernel_kind, double p0,
+                         double p1, double R, int32_t n_e, const double* e, double* rho,
+                         void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TBK_H */

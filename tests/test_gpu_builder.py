@@ -1,0 +1,190 @@
+"""Device Hamiltonian builder vs the oracle's setFromTriplets restatement:
+structure (col_ptr, row_idx) bit-exact; values bit-exact except where a Peierls
+phase goes through cos/sin (CUDA vs libm, compared to a few ulp)."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as orc
+from helpers import landau_gauge, spec_from, with_onsite_zeros
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+MODE = {"sparse": orc.MODE_SPARSE, "periodic": orc.MODE_PERIODIC_BARE, "bare": orc.MODE_BARE}
+
+
+def _build_both(tb, cell, span, mode, cplx, extend=None, gauge=None, scalar=None, disorder=None, removed=None):
+    X = tb.PartialLattice(cell, span)
+    N = X.get_total_number()
+    glin = None
+    if gauge is not None:
+        G, c = gauge
+        X.set_gauge_linear(G, c)
+        glin = np.concatenate([np.asarray(G).reshape(-1), c])
+    V = None
+    ocell = cell
+    if scalar is not None:
+        X.set_scalar_values(scalar)
+        V = scalar
+        ocell = with_onsite_zeros(cell)
+    if disorder is not None:
+        W, seed = disorder
+        X.set_scalar_disorder(W, seed)
+        V = orc.uniform_disorder(N, W, seed)
+        ocell = with_onsite_zeros(cell)
+    if removed is not None:
+        X.remove_sites(removed)
+    scalar_t = complex if cplx else float
+    if mode == "sparse":
+        H = X.get_Hamiltonian_sparse(scalar_t)
+    elif mode == "periodic":
+        H = X.get_Hamiltonian_periodic_extend_bare_sparse(extend, scalar_t)
+    else:
+        H = X.get_Hamiltonian_bare_sparse(scalar_t)
+    spec = spec_from(ocell if mode != "bare" else cell, span, mode=MODE[mode], is_complex=cplx, extend=extend,
+                     gauge_linear=glin if mode != "bare" else None, scalar_site=V if mode != "bare" else None,
+                     removed=None if removed is None else removed.astype(np.int32))
+    ref = orc.build_csc(spec)
+    return H, ref
+
+
+def _assert_same(H, ref, exact_values=True):
+    cp, ri, v = H.to_csc()
+    rcp, rri, rv = ref
+    assert np.array_equal(cp, rcp)
+    assert np.array_equal(ri, rri)
+    if exact_values:
+        assert np.array_equal(v, rv)
+    else:
+        assert np.max(np.abs(v - rv)) <= 4e-16 * max(1.0, np.max(np.abs(rv)))
+
+
+CASES = [
+    # id, model factory, span, mode, complex, extend, extras
+    ("square_pbc", lambda tb: tb.Square().add_hopping("A", 1, 1.0), (16, 12), "periodic", False, [1, 1], {}),
+    ("square_2x2_pbc_duplicates", lambda tb: tb.Square().add_hopping("A", 1, 1.0), (2, 2), "periodic", True, [1, 1], {}),
+    ("square_1x3_self_hops", lambda tb: tb.Square().add_hopping("A", 1, 0.7), (1, 3), "periodic", True, [1, 1], {}),
+    ("square_open", lambda tb: tb.Square().add_hopping("A", 1, 1.0), (9, 7), "sparse", False, None, {}),
+    ("honeycomb_open", lambda tb: tb.Honeycomb().add_hopping("A", 1, -2.7), (8, 6), "sparse", True, None, {}),
+    ("kagome_open", lambda tb: _kagome(tb), (5, 6), "sparse", False, None, {}),
+    ("lieb_pbc", lambda tb: tb.Lieb().add_hopping("A", 1, 1.0), (6, 5), "periodic", False, [1, 1], {}),
+    ("fcc_pbc", lambda tb: tb.FCC().add_hopping("A", 1, 1.0), (4, 5, 3), "periodic", False, [1, 1, 1], {}),
+    ("cubic_mixed_bc", lambda tb: tb.Cubic().add_hopping("A", 1, 1.0), (4, 3, 5), "periodic", True, [1, 0, 1], {}),
+    ("chain_pbc", lambda tb: tb.Chain().add_hopping("A", 1, 1.0), (10,), "periodic", False, [1], {}),
+    ("ti_sp_complex", lambda tb: tb.TI_sp(), (5, 4), "sparse", True, None, {}),
+    ("ti_sp_bare", lambda tb: tb.TI_sp(), (5, 4), "bare", True, None, {}),
+    ("sawtooth", lambda tb: tb.sawtooth_chain_p(0.25, 0.3535), (12,), "sparse", False, None, {}),
+    ("stub_pbc", lambda tb: tb.stub_1d_p(1.0, 0.5), (9,), "periodic", True, [1], {}),
+]
+
+
+def _kagome(tb):
+    k = tb.Kagome()
+    for a in "ABC":
+        k.add_hopping(a, 1, 1.0)
+    return k
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_builder_structure_and_values(gpu, case):
+    tb = gpu
+    _, factory, span, mode, cplx, extend, extra = case
+    H, ref = _build_both(tb, factory(tb), span, mode, cplx, extend=extend, **extra)
+    _assert_same(H, ref)
+
+
+def test_builder_disorder_on_device(gpu):
+    tb = gpu
+    cell = tb.Honeycomb().add_hopping("A", 1, -2.7)
+    H, ref = _build_both(tb, cell, (16, 16), "periodic", False, extend=[1, 1], disorder=(1.0, 1))
+    _assert_same(H, ref)   # counter-based RNG: identical draws on host and device
+
+
+def test_builder_scalar_field_values(gpu):
+    tb = gpu
+    cell = tb.Square().add_hopping("A", 1, 1.0)
+    V = np.linspace(-0.3, 0.4, 8 * 8)
+    H, ref = _build_both(tb, cell, (8, 8), "sparse", True, scalar=V)
+    _assert_same(H, ref)
+
+
+@pytest.mark.parametrize("mode,extend", [("sparse", None), ("periodic", [0, 1])])
+def test_builder_landau_gauge(gpu, mode, extend):
+    tb = gpu
+    cell = tb.Square().add_hopping("A", 1, 1.0)
+    H, ref = _build_both(tb, cell, (12, 10), mode, True, extend=extend, gauge=landau_gauge(2 * np.pi / 64))
+    _assert_same(H, ref, exact_values=False)
+    # Hermitian
+    M = H.to_scipy()
+    assert abs(M - M.conj().T).max() < 1e-15
+
+
+def test_builder_gauge_per_site(gpu):
+    tb = gpu
+    cell = tb.Honeycomb().add_hopping("A", 1, 1.0)
+    X = tb.PartialLattice(cell, (6, 5))
+    B = 0.05
+    X.set_gauge_field(lambda r: np.stack([-B * r[:, 1] / 2, B * r[:, 0] / 2, 0 * r[:, 0]], axis=1))
+    H = X.get_Hamiltonian_sparse(complex)
+    A = np.stack([-B * X.site_positions()[:, 1] / 2, B * X.site_positions()[:, 0] / 2,
+                  0 * X.site_positions()[:, 0]], axis=1)
+    ref = orc.build_csc(spec_from(cell, (6, 5), mode=orc.MODE_SPARSE, is_complex=True, gauge_site=A))
+    _assert_same(H, ref, exact_values=False)
+
+
+def test_builder_vacancies(gpu):
+    tb = gpu
+    cell = tb.Honeycomb().add_hopping("A", 1, 1.0)
+    rng = np.random.default_rng(5)
+    removed = (rng.random(2 * 7 * 6) < 0.2).astype(np.uint8)
+    H, ref = _build_both(tb, cell, (7, 6), "sparse", False, removed=removed)
+    _assert_same(H, ref)
+
+
+def test_rescale_and_commutator_bit_exact(gpu):
+    tb = gpu
+    cell = tb.Square().add_hopping("A", 1, 1.0)
+    X = tb.PartialLattice(cell, (9, 8))
+    H = X.get_Hamiltonian_sparse(complex)
+    G = tb.GreenFunction(16, H, -4.1, 4.3)
+    cp, ri, v = H.to_csc()
+    ref = orc.rescale_csc(len(cp) - 1, cp, ri, v, G.a, G.b)
+    got = G.scaled_HE.to_csc()
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+    # velocity: X H~ - H~ X (TB/snippets.h:316) and op_velocity (real, open BC)
+    Xop = X.op_position(0)
+    xd = orc.position_diag(spec_from(cell, (9, 8)), 0)
+    assert np.array_equal(Xop.to_csc()[2], xd)
+    V = tb.commutator(G.scaled_HE, Xop)
+    cpv, riv, vv = V.to_csc()
+    assert np.array_equal(cpv, ref[0]) and np.array_equal(riv, ref[1])
+    assert np.array_equal(vv, orc.commutator_values(len(cp) - 1, ref[0], ref[1], ref[2], xd))
+    vel = X.op_velocity(1)
+    Hr = X.get_Hamiltonian_sparse(float).to_csc()
+    yd = orc.position_diag(spec_from(cell, (9, 8)), 1)
+    assert np.array_equal(vel.to_csc()[2], orc.commutator_values(len(cp) - 1, Hr[0], Hr[1], Hr[2], yd))
+
+
+def test_config_sizes_counts(gpu):
+    tb = gpu
+    counts = json.loads((GOLD / "counts.json").read_text())
+    X = tb.PartialLattice(tb.Honeycomb().add_hopping("A", 1, -2.7), (1024, 1024))
+    X.set_scalar_disorder(1.0, 1)
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], float)
+    c = counts["honeycomb_1024x1024_pbc_disorder"]
+    assert H.shape[0] == c["N"] and H.nnz == c["nnz_H"]
+    G = tb.GreenFunction(8, H, -8.2, 8.2)
+    assert G.scaled_HE.nnz == c["nnz_Ht"]
+    X2 = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (256, 256))
+    H2 = X2.get_Hamiltonian_periodic_extend_bare_sparse([0, 1], complex)
+    c2 = counts["square_256x256_openx_pbcy"]
+    assert H2.nnz == c2["nnz_H"]
+    assert tb.GreenFunction(8, H2, -4.1, 4.1).scaled_HE.nnz == c2["nnz_Ht"]
+    X3 = tb.PartialLattice(tb.FCC().add_hopping("A", 1, 1.0), (128, 128, 128))
+    X3.set_scalar_disorder(2.0, 4)
+    H3 = X3.get_Hamiltonian_periodic_extend_bare_sparse([1, 1, 1], float)
+    assert H3.nnz == counts["fcc_128_pbc_disorder"]["nnz_H"]

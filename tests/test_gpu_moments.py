@@ -1,0 +1,170 @@
+"""Chebyshev moments on the GPU vs the FP64 oracle on the same seeded inputs.
+
+Tolerances (stated, relative to mu_0 = Re tr(bras^dagger kets)):
+  FP64 drop-in (complex128 recursion)           <= 1e-10
+  FP64 with moment doubling                     <= 1e-10
+  mixed precision (complex64 recursion, FP64
+  moment sums), M <= 256                        <= MIXED_TOL
+"""
+import numpy as np
+import pytest
+
+import oracle as orc
+from helpers import landau_gauge, spec_from, with_onsite_zeros
+
+pytestmark = pytest.mark.gpu
+MIXED_TOL = 2e-5
+
+
+def _system(tb, kind="square", L=(16, 16), cplx=False, disorder=None, gauge=None):
+    if kind == "square":
+        cell = tb.Square().add_hopping("A", 1, 1.0)
+    elif kind == "honeycomb":
+        cell = tb.Honeycomb().add_hopping("A", 1, -2.7)
+    else:
+        cell = tb.FCC().add_hopping("A", 1, 1.0)
+    X = tb.PartialLattice(cell, L)
+    if disorder:
+        X.set_scalar_disorder(*disorder)
+    if gauge is not None:
+        X.set_gauge_linear(*gauge)
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1] * len(L), complex if cplx else float)
+    return X, H
+
+
+def _rescaled_csc(tb, H, a, b=0.0):
+    G = tb.GreenFunction(8, H, b - a, b + a)
+    cp, ri, v = G.scaled_HE.to_csc()
+    return G, cp, ri, v
+
+
+def _err(mu, ref):
+    return float(np.max(np.abs(mu - ref)) / abs(ref[0]))
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_dropin_fp64_c1_config(gpu, cplx):
+    tb = gpu
+    # square 64x64 periodic, t = 1, bounds +-4.05, M = 256, R = 8, seed 0
+    X, H = _system(tb, "square", (64, 64), cplx)
+    G, cp, ri, v = _rescaled_csc(tb, H, 4.05)
+    n = len(cp) - 1
+    kets = tb.bases_of_uniform_ampl_with_random_phases(n, 8, 0)
+    mu = tb.Cheb_first_kind_seq_braket((n, cp, ri, v), 256, kets, kets, precision="fp64")
+    ref = orc.cheb_moments(n, cp, ri, v, 256, kets, kets)
+    assert _err(mu, ref) <= 1e-10
+    assert abs(mu[0] - 8.0) < 1e-12
+
+
+def test_dropin_fp64_bras_ne_kets_complex_gauge(gpu):
+    tb = gpu
+    X, H = _system(tb, "honeycomb", (10, 9), True, disorder=(1.0, 1), gauge=landau_gauge(2 * np.pi / 23))
+    G, cp, ri, v = _rescaled_csc(tb, H, 9.0, 0.05)
+    n = len(cp) - 1
+    kets = orc.random_phase_kets(n, 5, 3)
+    bras = orc.random_phase_kets(n, 5, 4)
+    mu = tb.Cheb_first_kind_seq_braket((n, cp, ri, v), 64, bras, kets, precision="fp64")
+    ref = orc.cheb_moments(n, cp, ri, v, 64, bras, kets)
+    assert np.max(np.abs(mu - ref)) <= 1e-10 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("R", [1, 3, 8, 33, 40])
+def test_fp64_r_chunking_and_padding(gpu, R):
+    tb = gpu
+    X, H = _system(tb, "square", (12, 10), False, disorder=(0.5, 2))
+    G, cp, ri, v = _rescaled_csc(tb, H, 4.5)
+    n = len(cp) - 1
+    kets = orc.random_phase_kets(n, R, 9)
+    mu = tb.Cheb_first_kind_seq_braket((n, cp, ri, v), 33, kets, kets, precision="fp64")
+    ref = orc.cheb_moments(n, cp, ri, v, 33, kets, kets)
+    assert _err(mu, ref) <= 1e-10
+
+
+@pytest.mark.parametrize("n_mom", [2, 3, 17, 64])
+def test_fp64_doubling_matches_oracle(gpu, n_mom):
+    tb = gpu
+    X, H = _system(tb, "honeycomb", (8, 8), False, disorder=(1.0, 1))
+    G, cp, ri, v = _rescaled_csc(tb, H, 8.5)
+    n = len(cp) - 1
+    kets = orc.random_phase_kets(n, 4, 1)
+    mu = tb.Cheb_first_kind_seq_braket((n, cp, ri, v), n_mom, kets, kets, precision="fp64", doubling=True)
+    ref = orc.cheb_moments(n, cp, ri, v, n_mom, kets, kets)
+    assert _err(mu, ref) <= 1e-10
+
+
+@pytest.mark.parametrize("name,model,span,t", [("square_L16_t1", "Square", (16, 16), 1.0),
+                                               ("honeycomb_L12_t-2.7", "Honeycomb", (12, 12), -2.7),
+                                               ("fcc_L6_t1", "FCC", (6, 6, 6), 1.0)])
+def test_fp64_exact_trace_golden(gpu, name, model, span, t):
+    tb = gpu
+    from pathlib import Path
+    gold = np.load(Path(__file__).resolve().parent / "golden" / "exact_moments.npz")
+    mu_exact, a = gold[name], float(gold[name + "__a"][0])
+    X = tb.PartialLattice(getattr(tb, model)().add_hopping("A", 1, t), span)
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1] * len(span), float)
+    G = tb.GreenFunction(len(mu_exact), H, -a, a)
+    n = H.shape[0]
+    eye = np.asfortranarray(np.eye(n, dtype=np.complex128))
+    solver = tb.KpmSolver(G.scaled_HE, n, precision="fp64", doubling=False)
+    mu = solver.run(len(mu_exact), eye, eye)
+    assert np.max(np.abs(mu - mu_exact)) / mu_exact[0] <= 1e-10
+
+
+@pytest.mark.parametrize("cplx,R", [(False, 8), (True, 8), (False, 32), (False, 1), (False, 64)])
+def test_mixed_precision_bound(gpu, cplx, R):
+    tb = gpu
+    X, H = _system(tb, "square", (64, 64), cplx, disorder=(0.5, 7))
+    G, cp, ri, v = _rescaled_csc(tb, H, 4.5)
+    n = len(cp) - 1
+    kets = orc.random_phase_kets(n, R, 0)
+    ref = orc.cheb_moments(n, cp, ri, v, 256, kets, kets)
+    for doubling in (False, True):
+        mu = tb.Cheb_first_kind_seq_braket((n, cp, ri, v), 256, kets, kets, precision="mixed", doubling=doubling)
+        assert _err(mu, ref) <= MIXED_TOL, (doubling, _err(mu, ref))
+
+
+def test_resident_plan_is_deterministic_and_random_kets(gpu):
+    tb = gpu
+    X, H = _system(tb, "honeycomb", (32, 32), False, disorder=(1.0, 1))
+    G, cp, ri, v = _rescaled_csc(tb, H, 8.5)
+    n = len(cp) - 1
+    s = tb.KpmSolver(G.scaled_HE, 16, precision="mixed", doubling=True)
+    a = s.run_random(128, 5)
+    b = s.run_random(128, 5)
+    assert np.array_equal(a, b)
+    kets = orc.random_phase_kets(n, 16, 5)        # same seeded kets, generated on the host
+    ref = orc.cheb_moments(n, cp, ri, v, 128, kets, kets)
+    assert _err(a, ref) <= MIXED_TOL
+    f = tb.KpmSolver(G.scaled_HE, 16, precision="fp64", doubling=True)
+    assert _err(f.run_random(128, 5), ref) <= 1e-10
+    ms, launches, bytes_ = s.last_timing()
+    assert launches == 64 and ms > 0 and bytes_ > 0
+
+
+def test_errors(gpu):
+    tb = gpu
+    X, H = _system(tb, "square", (4, 4), False)
+    G, cp, ri, v = _rescaled_csc(tb, H, 4.5)
+    n = len(cp) - 1
+    kets = orc.random_phase_kets(n, 2, 0)
+    with pytest.raises(tb.TbkError):
+        tb.Cheb_first_kind_seq_braket((n, cp, ri, v), 1, kets, kets)
+    with pytest.raises(ValueError):
+        tb.Cheb_first_kind_seq_braket((n, cp, ri, v), 8, orc.random_phase_kets(n, 2, 1), kets, doubling=True)
+    with pytest.raises(tb.TbkError):
+        tb.Cheb_first_kind_seq_braket((0, np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0)), 8,
+                                      np.zeros((0, 1), complex), np.zeros((0, 1), complex))
+
+
+def test_large_mixed_properties(gpu):
+    """Benchmark-size system (honeycomb 1024^2, R = 32): size-independent checks."""
+    tb = gpu
+    X, H = _system(tb, "honeycomb", (1024, 1024), False, disorder=(1.0, 1))
+    G = tb.GreenFunction(64, H, -8.6, 8.6)
+    s = tb.KpmSolver(G.scaled_HE, 32, precision="mixed", doubling=True)
+    f = tb.KpmSolver(G.scaled_HE, 32, precision="fp64", doubling=False)
+    mu = s.run_random(64, 1)
+    ref = f.run_random(64, 1)
+    assert abs(ref[0] - 32.0) < 1e-9                      # normalised kets: mu_0 = R
+    assert np.all(np.abs(mu) <= 32.0 * (1 + 1e-6))         # |T_n| <= 1 on the rescaled spectrum
+    assert _err(mu, ref) <= MIXED_TOL

@@ -1,0 +1,14 @@
+"""GB300 (sm_103a) kernel-polynomial hot path of chenzehan/tight_binding.
+
+The compute lives in libtbk (C ABI in include/tbk.h, CUDA in csrc/); this
+package mirrors the reference's model and KPM API on top of it.
+"""
+from . import capi
+from .capi import TbkError, device_count
+from .lattice import (Chain, Cubic, FCC, Honeycomb, Kagome, Lieb, PartialLattice, SparseMatrix, Square, TI_sp,
+                      UnitCell, commutator, graphene, sawtooth_chain_p, sawtooth_chain_X, stub_1d_p, stub_1d_X)
+from .kpm import (Cheb_first_kind_seq_braket, Dirichlet, Fejer, GreenFunction, GreenFunctionImag, Jackson,
+                  KpmSolver, Kernel, Lanczos, Lorentz, Wang_and_Zunger, bases_of_uniform_ampl_with_random_phases,
+                  density_of_states_function, density_of_states_seq, dos_from_moments, kernel_seq)
+
+__all__ = [n for n in dir() if not n.startswith("_")]

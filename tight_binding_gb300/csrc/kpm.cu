@@ -1,0 +1,620 @@
+// kpm.cu — Chebyshev (KPM) moments on sm_103a.
+//
+// Replaces cuda::Cheb_first_kind_seq_braket (TB/numerics_cuda.cu:190-323): the
+// reference runs one cuSPARSE SpMM (two for real H) plus one blocking cuBLAS dot
+// per moment.  Here one fused kernel per recursion step
+//     v_{n+1} = 2 H~ v_n - v_{n-1}      (v_1 = H~ v_0 on the first step)
+// streams the block of R vectors once, gathers the neighbours' 128-bit vector
+// slices through L1/L2, writes v_{n+1} over v_{n-1} in place, and folds the
+// moment dot products into the same pass with warp-shuffle reductions.  Per-CTA
+// FP64 partial sums go to a small buffer; one reduction at the end sums them in
+// a fixed order (deterministic, no atomics).
+//
+// Vector blocks are site-major: the R vectors of one site are contiguous (256 B
+// for R = 32 complex64), so every gathered neighbour is one coalesced row.
+//
+// Two precisions:
+//   TBK_PREC_FP64 : complex128 vectors, FP64 H~ (the plain drop-in)
+//   TBK_PREC_MIXED: complex64 vectors, FP32 H~, FP32 per-thread sums promoted
+//                   to FP64 for every reduction above the thread.
+// With bras == kets (DoS) the Chebyshev product rule gives two moments per step:
+//   mu_2n = 2 <v_n|v_n> - mu_0,   mu_2n+1 = 2 <v_n+1|v_n> - mu_1.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "host_model.h"
+#include "tbk_internal.h"
+
+namespace tbk {
+
+template <typename F> struct C2;
+template <> struct C2<float> { using T = float2; };
+template <> struct C2<double> { using T = double2; };
+
+// Lane slice of a site's R vectors: VPL complex values moved as one access.
+template <typename F, int VPL>
+struct LaneV {
+  F re[VPL], im[VPL];
+};
+
+template <typename F, int VPL>
+__device__ __forceinline__ LaneV<F, VPL> ld_ro(const typename C2<F>::T* p) {
+  LaneV<F, VPL> o;
+  if constexpr (sizeof(F) == 4 && VPL == 2) {
+    float4 q = __ldg(reinterpret_cast<const float4*>(p));
+    o.re[0] = q.x; o.im[0] = q.y; o.re[1] = q.z; o.im[1] = q.w;
+  } else {
+    auto q = __ldg(p);
+    o.re[0] = q.x; o.im[0] = q.y;
+  }
+  return o;
+}
+template <typename F, int VPL>
+__device__ __forceinline__ LaneV<F, VPL> ld_stream(const typename C2<F>::T* p) {
+  LaneV<F, VPL> o;
+  if constexpr (sizeof(F) == 4 && VPL == 2) {
+    float4 q = __ldcs(reinterpret_cast<const float4*>(p));
+    o.re[0] = q.x; o.im[0] = q.y; o.re[1] = q.z; o.im[1] = q.w;
+  } else {
+    auto q = __ldcs(p);
+    o.re[0] = q.x; o.im[0] = q.y;
+  }
+  return o;
+}
+template <typename F, int VPL>
+__device__ __forceinline__ void st_v(typename C2<F>::T* p, const LaneV<F, VPL>& v) {
+  if constexpr (sizeof(F) == 4 && VPL == 2) {
+    *reinterpret_cast<float4*>(p) = make_float4(v.re[0], v.im[0], v.re[1], v.im[1]);
+  } else {
+    typename C2<F>::T q;
+    q.x = v.re[0]; q.y = v.im[0];
+    *p = q;
+  }
+}
+
+template <typename F, bool CPLX_H>
+struct HVal;
+template <typename F>
+struct HVal<F, false> {
+  F v;
+  __device__ __forceinline__ static HVal load(const F* p, int64_t o) { return HVal{__ldg(p + o)}; }
+  template <int VPL>
+  __device__ __forceinline__ void fma(const LaneV<F, VPL>& x, LaneV<F, VPL>& acc) const {
+#pragma unroll
+    for (int q = 0; q < VPL; ++q) { acc.re[q] = fma_(v, x.re[q], acc.re[q]); acc.im[q] = fma_(v, x.im[q], acc.im[q]); }
+  }
+  __device__ __forceinline__ static F fma_(F a, F b, F c) { return a * b + c; }
+};
+template <typename F>
+struct HVal<F, true> {
+  F r, i;
+  __device__ __forceinline__ static HVal load(const F* p, int64_t o) {
+    auto q = __ldg(reinterpret_cast<const typename C2<F>::T*>(p) + o);
+    return HVal{q.x, q.y};
+  }
+  template <int VPL>
+  __device__ __forceinline__ void fma(const LaneV<F, VPL>& x, LaneV<F, VPL>& acc) const {
+#pragma unroll
+    for (int q = 0; q < VPL; ++q) {
+      acc.re[q] = r * x.re[q] + acc.re[q];
+      acc.re[q] = -i * x.im[q] + acc.re[q];
+      acc.im[q] = r * x.im[q] + acc.im[q];
+      acc.im[q] = i * x.re[q] + acc.im[q];
+    }
+  }
+};
+
+template <typename F> struct VecW { static constexpr int max_vpl = (sizeof(F) == 4) ? 2 : 1; };
+
+constexpr int kStepThreads = 256;
+constexpr int kStepWarps = kStepThreads / 32;
+
+// One recursion step over all rows.
+//   FIRST: y = H x                    else: y = 2 H x - y (y holds v_{n-1})
+//   BRAS == nullptr (doubling):   part[0] += <x|x>,  part[1] += <x|y>
+//   BRAS != nullptr (braket):     part[0] += <b|y>;  FIRST also part[1] += <b|x>
+template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET>
+__global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
+    int32_t n, int32_t n_tiles, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
+    const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
+    typename C2<F>::T* y, const typename C2<F>::T* __restrict__ bras, double* __restrict__ part,
+    int store, int reverse) {
+  using CT = typename C2<F>::T;
+  constexpr int VPL = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
+  constexpr int LPR = R / VPL;             // lanes per row
+  constexpr int RPW = 32 / LPR;            // rows per warp
+  constexpr int ROWS_PER_TILE = RPW * kStepWarps;
+  static_assert(LPR >= 1 && LPR <= 32 && (32 % LPR) == 0, "R out of range");
+  using Acc = F;                           // per-thread sums in the vector precision
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane % LPR;
+  Acc m0 = 0, m1 = 0;
+
+  for (int32_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const int32_t tile = reverse ? (n_tiles - 1 - t) : t;
+    const int32_t r = tile * ROWS_PER_TILE + warp * RPW + lane / LPR;
+    if (r >= n) continue;
+    const int64_t me = (int64_t)r * LPR + sub;
+    const LaneV<F, VPL> xs = ld_ro<F, VPL>(x + me * VPL);
+    LaneV<F, VPL> prev;
+    if constexpr (!FIRST) prev = ld_stream<F, VPL>(y + me * VPL);
+    LaneV<F, VPL> acc;
+#pragma unroll
+    for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
+    HVal<F, CPLX_H>::load(diag, r).template fma<VPL>(xs, acc);
+    const int32_t s = r >> 5, l = r & 31;
+    const int32_t off = soff[s];
+    const int32_t w = (soff[s + 1] - off) >> 5;
+    const int32_t* cp = ecol + off + l;
+    int k = 0;
+    for (; k + 4 <= w; k += 4) {
+      int32_t c[4];
+      HVal<F, CPLX_H> h[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) { c[u] = __ldg(cp + (k + u) * 32); h[u] = HVal<F, CPLX_H>::load(eval, off + l + (int64_t)(k + u) * 32); }
+      LaneV<F, VPL> xv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) xv[u] = ld_ro<F, VPL>(x + ((int64_t)c[u] * LPR + sub) * VPL);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
+    }
+    for (; k < w; ++k) {
+      int32_t c = __ldg(cp + k * 32);
+      HVal<F, CPLX_H> h = HVal<F, CPLX_H>::load(eval, off + l + (int64_t)k * 32);
+      LaneV<F, VPL> xv = ld_ro<F, VPL>(x + ((int64_t)c * LPR + sub) * VPL);
+      h.template fma<VPL>(xv, acc);
+    }
+    LaneV<F, VPL> out;
+#pragma unroll
+    for (int q = 0; q < VPL; ++q) {
+      if constexpr (FIRST) { out.re[q] = acc.re[q]; out.im[q] = acc.im[q]; }
+      else { out.re[q] = F(2) * acc.re[q] - prev.re[q]; out.im[q] = F(2) * acc.im[q] - prev.im[q]; }
+    }
+    if (store) st_v<F, VPL>(y + me * VPL, out);
+    if constexpr (BRAKET) {
+      const LaneV<F, VPL> b = ld_ro<F, VPL>(bras + me * VPL);
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) {
+        m0 += b.re[q] * out.re[q] + b.im[q] * out.im[q];
+        if constexpr (FIRST) m1 += b.re[q] * xs.re[q] + b.im[q] * xs.im[q];
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) {
+        m0 += xs.re[q] * xs.re[q] + xs.im[q] * xs.im[q];
+        m1 += xs.re[q] * out.re[q] + xs.im[q] * out.im[q];
+      }
+    }
+  }
+  // FP64 from here on: warp shuffle, then across the CTA's warps
+  double d0 = (double)m0, d1 = (double)m1;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+    d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+  }
+  __shared__ double sh[2][kStepWarps];
+  if (lane == 0) { sh[0][warp] = d0; sh[1][warp] = d1; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+#pragma unroll
+    for (int q = 0; q < kStepWarps; ++q) { a += sh[0][q]; b += sh[1][q]; }
+    part[blockIdx.x] = a;
+    part[gridDim.x + blockIdx.x] = b;
+  }
+}
+
+// Column-major complex128 (Eigen) -> site-major work block of width Rp.
+template <typename F>
+__global__ void load_block_kernel(int32_t n, int32_t R, int32_t r0, int32_t rc, int32_t Rp,
+                                  const double2* __restrict__ src, typename C2<F>::T* __restrict__ dst) {
+  __shared__ double2 tile[32][33];
+  const int32_t i0 = blockIdx.x * 32;
+  const int32_t c0 = blockIdx.y * 32;
+  // read: consecutive threads walk consecutive sites of one vector
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int32_t c = c0 + k, i = i0 + threadIdx.x;
+    double2 v = make_double2(0.0, 0.0);
+    if (c < rc && i < n && r0 + c < R) v = src[(int64_t)(r0 + c) * n + i];
+    tile[k][threadIdx.x] = v;
+  }
+  __syncthreads();
+  // write: consecutive threads walk consecutive vectors of one site
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    int32_t i = i0 + k, c = c0 + threadIdx.x;
+    if (i < n && c < Rp) {
+      double2 v = tile[threadIdx.x][k];
+      typename C2<F>::T o;
+      o.x = (F)v.x; o.y = (F)v.y;
+      dst[(int64_t)i * Rp + c] = o;
+    }
+  }
+}
+
+// Device random-phase kets exp(2 pi i u)/sqrt(N), u = u01(seed, r, i), site-major.
+template <typename F>
+__global__ void random_block_kernel(int32_t n, int32_t R, int32_t r0, int32_t Rp, uint64_t seed,
+                                    typename C2<F>::T* __restrict__ dst) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (int64_t)n * Rp) return;
+  int32_t i = (int32_t)(g / Rp), c = (int32_t)(g % Rp);
+  typename C2<F>::T o;
+  if (r0 + c < R) {
+    double th = 6.283185307179586476925286766559 * u01(seed, (uint64_t)(r0 + c), (uint64_t)i);
+    double s, cs;
+    sincos(th, &s, &cs);
+    double inv = 1.0 / sqrt((double)n);
+    o.x = (F)(cs * inv); o.y = (F)(s * inv);
+  } else {
+    o.x = 0; o.y = 0;
+  }
+  dst[g] = o;
+}
+
+// Fixed-order sum of the per-CTA partials of every (chunk, step, slot).
+__global__ void reduce_partials_kernel(const double* __restrict__ part, int32_t n_chunks, int32_t n_steps,
+                                       int32_t nblk, double* __restrict__ sums) {
+  const int32_t step = blockIdx.x, slot = blockIdx.y;
+  double acc = 0.0;
+  __shared__ double sh[256];
+  for (int32_t ch = 0; ch < n_chunks; ++ch) {
+    const double* p = part + (((int64_t)ch * n_steps + step) * 2 + slot) * nblk;
+    double a = 0.0;
+    for (int32_t b = threadIdx.x; b < nblk; b += blockDim.x) a += p[b];
+    sh[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) acc += sh[0];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sums[step * 2 + slot] = acc;
+}
+
+// Assemble mu_k (FP64) from the step sums.
+__global__ void assemble_moments_kernel(const double* __restrict__ sums, int32_t n_mom, int32_t doubling,
+                                        double* __restrict__ mu) {
+  int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_mom) return;
+  if (doubling) {
+    const double mu0 = sums[0], mu1 = sums[1];
+    int32_t s = k >> 1;
+    if (k == 0) mu[k] = mu0;
+    else if (k == 1) mu[k] = mu1;
+    else mu[k] = (k & 1) ? 2.0 * sums[2 * s + 1] - mu1 : 2.0 * sums[2 * s] - mu0;
+  } else {
+    // step 0 holds <b|v1> in slot 0 and <b|v0> in slot 1; step s>0 holds <b|v_{s+1}>
+    if (k == 0) mu[k] = sums[1];
+    else mu[k] = sums[2 * (k - 1)];
+  }
+}
+
+// ----------------------------------------------------------------- dispatch
+struct StepArgs {
+  int32_t n, n_tiles;
+  const int32_t* soff;
+  const int32_t* ecol;
+  const void* eval;
+  const void* diag;
+  const void* x;
+  void* y;
+  const void* bras;
+  double* part;
+  int store, reverse;
+};
+
+template <typename F, int R, bool CPLX_H>
+static int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, cudaStream_t st) {
+  using CT = typename C2<F>::T;
+  auto x = static_cast<const CT*>(a.x);
+  auto y = static_cast<CT*>(a.y);
+  auto b = static_cast<const CT*>(a.bras);
+  auto ev = static_cast<const F*>(a.eval);
+  auto dg = static_cast<const F*>(a.diag);
+#define TBK_STEP(FI, BR)                                                                   \
+  kpm_step_kernel<F, R, CPLX_H, FI, BR><<<grid, kStepThreads, 0, st>>>(                    \
+      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, b, a.part, a.store, a.reverse)
+  if (first) { if (braket) TBK_STEP(true, true); else TBK_STEP(true, false); }
+  else { if (braket) TBK_STEP(false, true); else TBK_STEP(false, false); }
+#undef TBK_STEP
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
+}
+
+template <typename F, bool CPLX_H>
+static int launch_step(int R, const StepArgs& a, bool first, bool braket, int grid, cudaStream_t st) {
+  switch (R) {
+    case 1: return launch_step_r<F, 1, CPLX_H>(a, first, braket, grid, st);
+    case 2: return launch_step_r<F, 2, CPLX_H>(a, first, braket, grid, st);
+    case 4: return launch_step_r<F, 4, CPLX_H>(a, first, braket, grid, st);
+    case 8: return launch_step_r<F, 8, CPLX_H>(a, first, braket, grid, st);
+    case 16: return launch_step_r<F, 16, CPLX_H>(a, first, braket, grid, st);
+    case 32: return launch_step_r<F, 32, CPLX_H>(a, first, braket, grid, st);
+    case 64:
+      if constexpr (sizeof(F) == 4) return launch_step_r<F, 64, CPLX_H>(a, first, braket, grid, st);
+      break;
+  }
+  return fail(TBK_ERR_UNSUPPORTED, "chunk width %d not instantiated", R);
+}
+
+template <typename F, bool CPLX_H, int R>
+static int occupancy_blocks() {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kpm_step_kernel<F, R, CPLX_H, false, false>, kStepThreads, 0);
+  return nb > 0 ? nb : 1;
+}
+
+static int rows_per_tile(int prec, int Rc) {
+  int vpl = prec == TBK_PREC_MIXED ? (Rc >= 2 ? 2 : 1) : 1;
+  int lpr = Rc / vpl;
+  return (32 / lpr) * kStepWarps;
+}
+
+}  // namespace tbk
+
+using namespace tbk;
+
+struct tbk_kpm_s {
+  tbk_sparse_s* H = nullptr;
+  int32_t R = 0, Rc = 0, n_chunks = 0, flags = 0, prec = 0;
+  int64_t n = 0;
+  size_t csize = 0;                 // bytes of one complex element
+  DevBuf va, vb, bras, stage, part, sums, mu;
+  int grid = 0, n_tiles = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0, last_bytes = 0.0;
+  int32_t last_launches = 0;
+  int32_t cap_steps = 0;            // partial buffer capacity (steps)
+};
+
+static int plan_partials(tbk_kpm_s* P, int32_t n_steps) {
+  if (n_steps <= P->cap_steps) return TBK_OK;
+  TBK_TRY(P->part.alloc(sizeof(double) * 2 * (size_t)n_steps * P->grid * P->n_chunks));
+  TBK_TRY(P->sums.alloc(sizeof(double) * 2 * (size_t)n_steps));
+  P->cap_steps = n_steps;
+  return TBK_OK;
+}
+
+static int plan_mu(tbk_kpm_s* P, int32_t n_mom) {
+  if (P->mu.bytes >= sizeof(double) * (size_t)n_mom) return TBK_OK;
+  return P->mu.alloc(sizeof(double) * n_mom);
+}
+
+// Runs all chunks.  kets_loader(r0, dst) fills the chunk's v0 (site-major);
+// bras_loader(r0, dst) fills the chunk's bras block (braket mode only).
+template <typename KL, typename BL>
+static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_loader, BL&& bras_loader,
+                        double* mu_out, bool mu_device, cudaStream_t st) {
+  if (n_mom < 2) return fail(TBK_ERR_INVALID, "n must be greater than or equal to 2");
+  const bool doubling = !braket;
+  const int32_t n_steps = doubling ? (n_mom + 1) / 2 : n_mom - 1;
+  TBK_TRY(plan_partials(P, n_steps));
+  TBK_TRY(plan_mu(P, n_mom));
+  if (braket && P->bras.bytes < P->va.bytes) TBK_TRY(P->bras.alloc(P->va.bytes));
+  const EllDev& E = P->H->ell;
+  const bool mixed = P->prec == TBK_PREC_MIXED;
+  const bool cplx = P->H->is_complex != 0;
+  float ms_total = 0.f;
+  int32_t launches = 0;
+  for (int32_t ch = 0; ch < P->n_chunks; ++ch) {
+    const int32_t r0 = ch * P->Rc;
+    TBK_TRY(kets_loader(r0, P->va.p));
+    if (braket) TBK_TRY(bras_loader(r0, P->bras.p));
+    TBK_CUDA(cudaEventRecord(P->ev0, st));
+    void* x = P->va.p;
+    void* y = P->vb.p;
+    for (int32_t s = 0; s < n_steps; ++s) {
+      StepArgs a;
+      a.n = (int32_t)P->n;
+      a.n_tiles = P->n_tiles;
+      a.soff = E.slice_off.as<int32_t>();
+      a.ecol = E.col.as<int32_t>();
+      a.eval = mixed ? E.val32.p : E.val64.p;
+      a.diag = mixed ? E.diag32.p : E.diag64.p;
+      a.x = x;
+      a.y = y;
+      a.bras = braket ? P->bras.p : nullptr;
+      a.part = P->part.as<double>() + (((int64_t)ch * n_steps + s) * 2) * P->grid;
+      a.store = (doubling && s == n_steps - 1) ? 0 : 1;
+      a.reverse = (P->flags & TBK_FLAG_NO_L2_ZIGZAG) ? 0 : (s & 1);
+      const bool first = s == 0;
+      int rc;
+      if (mixed) rc = cplx ? launch_step<float, true>(P->Rc, a, first, braket, P->grid, st)
+                           : launch_step<float, false>(P->Rc, a, first, braket, P->grid, st);
+      else rc = cplx ? launch_step<double, true>(P->Rc, a, first, braket, P->grid, st)
+                     : launch_step<double, false>(P->Rc, a, first, braket, P->grid, st);
+      if (rc != TBK_OK) return rc;
+      ++launches;
+      std::swap(x, y);   // y now holds v_{n+1}; it becomes x, x (v_n) becomes the next v_{n-1}
+    }
+    TBK_CUDA(cudaEventRecord(P->ev1, st));
+    TBK_CUDA(cudaEventSynchronize(P->ev1));
+    float ms = 0.f;
+    TBK_CUDA(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
+    ms_total += ms;
+  }
+  reduce_partials_kernel<<<dim3(n_steps, 2), 256, 0, st>>>(P->part.as<double>(), P->n_chunks, n_steps, P->grid,
+                                                          P->sums.as<double>());
+  TBK_CHECK_LAUNCH();
+  assemble_moments_kernel<<<(n_mom + 255) / 256, 256, 0, st>>>(P->sums.as<double>(), n_mom, doubling ? 1 : 0,
+                                                               P->mu.as<double>());
+  TBK_CHECK_LAUNCH();
+  if (mu_device) TBK_CUDA(cudaMemcpyAsync(mu_out, P->mu.p, sizeof(double) * n_mom, cudaMemcpyDeviceToDevice, st));
+  else TBK_CUDA(cudaMemcpyAsync(mu_out, P->mu.p, sizeof(double) * n_mom, cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  // algorithmic DRAM bytes per recursion launch (average over the launches)
+  const double vec = (double)P->n * P->Rc * P->csize;
+  const double hv = (mixed ? 4.0 : 8.0) * (cplx ? 2.0 : 1.0);
+  const double mat = (double)E.n_entries * (4.0 + hv) + (double)E.n_rows * hv + 4.0 * (E.n_slices + 1);
+  double per_chunk = 0.0;
+  for (int32_t s = 0; s < n_steps; ++s) {
+    double b = vec;                                        // x
+    if (s > 0) b += vec;                                   // v_{n-1}
+    if (!(doubling && s == n_steps - 1)) b += vec;         // y store
+    if (braket) b += vec;                                  // bras
+    per_chunk += b + mat;
+  }
+  P->last_ms = ms_total;
+  P->last_launches = launches;
+  P->last_bytes = launches ? per_chunk * P->n_chunks / launches : 0.0;
+  return TBK_OK;
+}
+
+extern "C" {
+
+int tbk_kpm_create(tbk_kpm* out, tbk_sparse Ht, int32_t R, int32_t flags) {
+  if (!out || !Ht) return fail(TBK_ERR_INVALID, "tbk_kpm_create: null argument");
+  *out = nullptr;
+  if (R < 1) return fail(TBK_ERR_INVALID, "R must be >= 1");
+  const int prec = flags & TBK_FLAG_PREC_MASK;
+  if (prec != TBK_PREC_FP64 && prec != TBK_PREC_MIXED) return fail(TBK_ERR_INVALID, "unknown precision %d", prec);
+  cudaStream_t st = nullptr;
+  TBK_TRY(ensure_ell(Ht, st));
+  auto* P = new tbk_kpm_s();
+  P->H = Ht;
+  P->R = R;
+  P->flags = flags;
+  P->prec = prec;
+  P->n = Ht->rows;
+  P->csize = prec == TBK_PREC_MIXED ? 8 : 16;
+  const int rmax = prec == TBK_PREC_MIXED ? 64 : 32;
+  int rc = 1;
+  while (rc < R && rc < rmax) rc <<= 1;
+  P->Rc = rc;
+  P->n_chunks = (R + rc - 1) / rc;
+  const int rpt = rows_per_tile(prec, rc);
+  P->n_tiles = (int)((P->n + rpt - 1) / rpt);
+  int occ = 1;
+  const bool cplx = Ht->is_complex != 0;
+#define OCC(F, C)                                                                 \
+  switch (rc) {                                                                   \
+    case 1: occ = occupancy_blocks<F, C, 1>(); break;                             \
+    case 2: occ = occupancy_blocks<F, C, 2>(); break;                             \
+    case 4: occ = occupancy_blocks<F, C, 4>(); break;                             \
+    case 8: occ = occupancy_blocks<F, C, 8>(); break;                             \
+    case 16: occ = occupancy_blocks<F, C, 16>(); break;                           \
+    default: occ = occupancy_blocks<F, C, 32>(); break;                           \
+  }
+  if (prec == TBK_PREC_MIXED) { if (cplx) { OCC(float, true) } else { OCC(float, false) } }
+  else { if (cplx) { OCC(double, true) } else { OCC(double, false) } }
+#undef OCC
+  P->grid = std::max(1, std::min(P->n_tiles, sm_count() * occ));
+  const size_t blk = (size_t)P->n * rc * P->csize;
+  int s;
+  if ((s = P->va.alloc(blk)) != TBK_OK || (s = P->vb.alloc(blk)) != TBK_OK) { delete P; return s; }
+  if (cudaEventCreate(&P->ev0) != cudaSuccess || cudaEventCreate(&P->ev1) != cudaSuccess) {
+    delete P;
+    return fail(TBK_ERR_CUDA, "cudaEventCreate failed");
+  }
+  *out = P;
+  return TBK_OK;
+}
+
+void tbk_kpm_destroy(tbk_kpm P) {
+  if (!P) return;
+  cudaDeviceSynchronize();
+  if (P->ev0) cudaEventDestroy(P->ev0);
+  if (P->ev1) cudaEventDestroy(P->ev1);
+  delete P;
+}
+
+int tbk_kpm_run(tbk_kpm P, int32_t n_mom, const double* bras, const double* kets, double* mu_out,
+                void* stream) {
+  if (!P || !kets || !bras || !mu_out) return fail(TBK_ERR_INVALID, "tbk_kpm_run: null argument");
+  cudaStream_t st = as_stream(stream);
+  const bool dev = (P->flags & TBK_FLAG_DEVICE_PTRS) != 0;
+  const bool doubling = (P->flags & TBK_FLAG_DOUBLING) != 0;
+  if (doubling && bras != kets) return fail(TBK_ERR_INVALID, "TBK_FLAG_DOUBLING needs bras == kets");
+  const bool same = bras == kets;
+  const size_t in_bytes = sizeof(double2) * (size_t)P->n * P->R;
+  // host inputs: one H2D copy each into staging; every chunk transposes its columns from there
+  const double2* kets_dev = reinterpret_cast<const double2*>(kets);
+  const double2* bras_dev = reinterpret_cast<const double2*>(bras);
+  if (!dev) {
+    const size_t need = same ? in_bytes : 2 * in_bytes;
+    if (P->stage.bytes < need) TBK_TRY(P->stage.alloc(need));
+    TBK_CUDA(cudaMemcpyAsync(P->stage.p, kets, in_bytes, cudaMemcpyHostToDevice, st));
+    kets_dev = P->stage.as<double2>();
+    bras_dev = kets_dev;
+    if (!same) {
+      TBK_CUDA(cudaMemcpyAsync(P->stage.as<char>() + in_bytes, bras, in_bytes, cudaMemcpyHostToDevice, st));
+      bras_dev = reinterpret_cast<const double2*>(P->stage.as<char>() + in_bytes);
+    }
+  }
+  const bool mixed = P->prec == TBK_PREC_MIXED;
+  auto load_from = [&](const double2* src) {
+    return [&, src](int32_t r0, void* dst) -> int {
+      dim3 g((unsigned)((P->n + 31) / 32), (unsigned)((P->Rc + 31) / 32)), b(32, 8);
+      int32_t rc = std::min(P->Rc, P->R - r0);
+      if (mixed) load_block_kernel<float><<<g, b, 0, st>>>((int32_t)P->n, P->R, r0, rc, P->Rc, src, static_cast<float2*>(dst));
+      else load_block_kernel<double><<<g, b, 0, st>>>((int32_t)P->n, P->R, r0, rc, P->Rc, src, static_cast<double2*>(dst));
+      TBK_CHECK_LAUNCH();
+      return TBK_OK;
+    };
+  };
+  return kpm_run_impl(P, n_mom, !doubling, load_from(kets_dev), load_from(bras_dev), mu_out, dev, st);
+}
+
+int tbk_kpm_run_random(tbk_kpm P, int32_t n_mom, uint64_t seed, double* mu_out, void* stream) {
+  if (!P || !mu_out) return fail(TBK_ERR_INVALID, "tbk_kpm_run_random: null argument");
+  cudaStream_t st = as_stream(stream);
+  const bool dev = (P->flags & TBK_FLAG_DEVICE_PTRS) != 0;
+  const bool mixed = P->prec == TBK_PREC_MIXED;
+  const bool doubling = (P->flags & TBK_FLAG_DOUBLING) != 0;
+  auto gen = [&](int32_t r0, void* dst) -> int {
+    int64_t tot = P->n * P->Rc;
+    if (mixed) random_block_kernel<float><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>((int32_t)P->n, P->R, r0, P->Rc, seed, static_cast<float2*>(dst));
+    else random_block_kernel<double><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>((int32_t)P->n, P->R, r0, P->Rc, seed, static_cast<double2*>(dst));
+    TBK_CHECK_LAUNCH();
+    return TBK_OK;
+  };
+  return kpm_run_impl(P, n_mom, !doubling, gen, gen, mu_out, dev, st);
+}
+
+int tbk_kpm_last_timing(tbk_kpm P, double* ms, int32_t* launches, double* bytes) {
+  if (!P) return fail(TBK_ERR_INVALID, "tbk_kpm_last_timing: null plan");
+  if (ms) *ms = P->last_ms;
+  if (launches) *launches = P->last_launches;
+  if (bytes) *bytes = P->last_bytes;
+  return TBK_OK;
+}
+
+static int cheb_braket_common(int32_t n_rows, int64_t nnz, const int32_t* cp, const int32_t* ri,
+                              const double* v, int cplx, int32_t n, const double* bras, const double* kets,
+                              int32_t R, int32_t flags, double* mu_out) {
+  if (!cp || !bras || !kets || !mu_out || (nnz > 0 && (!ri || !v)))
+    return fail(TBK_ERR_INVALID, "Cheb_first_kind_seq_braket: null argument");
+  if (n < 2) return fail(TBK_ERR_INVALID, "n must be greater than or equal to 2");
+  if (n_rows < 1 || R < 1) return fail(TBK_ERR_INVALID, "Cheb_first_kind_seq_braket: empty input");
+  if ((flags & TBK_FLAG_DOUBLING) && bras != kets)
+    return fail(TBK_ERR_INVALID, "TBK_FLAG_DOUBLING needs bras == kets");
+  tbk_sparse H = nullptr;
+  TBK_TRY(tbk_sparse_from_csc(&H, n_rows, n_rows, nnz, cp, ri, v, cplx, 0, nullptr));
+  tbk_kpm P = nullptr;
+  int s = tbk_kpm_create(&P, H, R, flags & ~TBK_FLAG_DEVICE_PTRS);
+  if (s == TBK_OK) s = tbk_kpm_run(P, n, bras, kets, mu_out, nullptr);
+  tbk_kpm_destroy(P);
+  tbk_sparse_destroy(H);
+  return s;
+}
+
+int tbk_cheb_braket_real(int32_t n_rows, int64_t nnz, const int32_t* cp, const int32_t* ri, const double* v,
+                         int32_t n, const double* bras, const double* kets, int32_t R, int32_t flags,
+                         double* mu_out) {
+  return cheb_braket_common(n_rows, nnz, cp, ri, v, 0, n, bras, kets, R, flags, mu_out);
+}
+
+int tbk_cheb_braket_complex(int32_t n_rows, int64_t nnz, const int32_t* cp, const int32_t* ri, const double* v,
+                            int32_t n, const double* bras, const double* kets, int32_t R, int32_t flags,
+                            double* mu_out) {
+  return cheb_braket_common(n_rows, nnz, cp, ri, v, 1, n, bras, kets, R, flags, mu_out);
+}
+
+}  // extern "C"

@@ -1,0 +1,96 @@
+// tbk_internal.h — shared internals of libtbk (device sparse objects, errors).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/tbk.h"
+
+namespace tbk {
+
+// ---- error handling: every C entry point returns a status and records a message
+void set_error(int code, const std::string& msg);
+int fail(int code, const char* fmt, ...);
+#define TBK_CUDA(call)                                                              \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      return ::tbk::fail(TBK_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,   \
+                         cudaGetErrorString(e_));                                   \
+  } while (0)
+#define TBK_CHECK_LAUNCH() TBK_CUDA(cudaGetLastError())
+#define TBK_TRY(expr)                                                               \
+  do {                                                                              \
+    int s_ = (expr);                                                                \
+    if (s_ != TBK_OK) return s_;                                                    \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ---- device buffer (RAII, cudaMalloc)
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
+  int alloc(size_t n) {
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) { p = nullptr; return fail(TBK_ERR_NOMEM, "cudaMalloc(%zu): %s", n, cudaGetErrorString(e)); }
+    bytes = n;
+    return TBK_OK;
+  }
+  template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// Sliced-ELL view of a square matrix for the recursion kernels: rows are cut in
+// slices of 32; slice s stores width_s entries per row, column-major inside the
+// slice (entry k of row 32*s + l at off[s] + 32*k + l).  The diagonal is kept
+// apart so that every row owns its v_n element.  Padding entries point at the
+// row itself with value 0.
+struct EllDev {
+  int32_t n_rows = 0, n_slices = 0;
+  int64_t n_entries = 0;
+  int32_t max_width = 0;
+  DevBuf slice_off;   // int32 [n_slices + 1]
+  DevBuf col;         // int32 [n_entries]
+  DevBuf val64;       // double / double2 [n_entries]
+  DevBuf diag64;      // double / double2 [n_rows]
+  DevBuf val32;       // float / float2 [n_entries]  (mixed precision)
+  DevBuf diag32;      // float / float2 [n_rows]
+};
+
+}  // namespace tbk
+
+// Device-resident sparse matrix: Eigen-compatible CSC (the reference-facing
+// form) plus the sliced-ELL of its rows used by the recursion kernels.
+struct tbk_sparse_s {
+  int32_t rows = 0, cols = 0;
+  int64_t nnz = 0;
+  int32_t is_complex = 0;
+  tbk::DevBuf col_ptr;   // int32 [cols+1]
+  tbk::DevBuf row_idx;   // int32 [nnz]
+  tbk::DevBuf values;    // double or double2 [nnz]
+  bool ell_ready = false;
+  tbk::EllDev ell;
+};
+
+namespace tbk {
+// builder.cu
+int ensure_ell(tbk_sparse_s* A, cudaStream_t st);
+int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t st, int32_t* total_host);
+int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st, int64_t* total_host);
+int sm_count();
+}  // namespace tbk
