@@ -353,6 +353,24 @@ def run_gpu(args):
     return 0
 
 
+def run_kernel_only(args):
+    """Small case of the same kernel for ncu captures: one mixed-precision DoS
+    solve (doubling) on a honeycomb of --cells^2 cells, R = 32."""
+    import tight_binding_gb300 as tb
+
+    X = tb.PartialLattice(tb.Honeycomb().add_hopping("A", 1, T_HOP), (args.cells, args.cells))
+    X.set_scalar_disorder(W_DIS, 1)
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], float)
+    G = tb.GreenFunction(args.moments, H, -BOUND, BOUND)
+    s = tb.KpmSolver(G.scaled_HE, R_VEC, precision=args.precision, doubling=args.precision == "mixed")
+    for _ in range(2):
+        mu = s.run_random(args.moments, 0)
+    ms, nl, b = s.last_timing()
+    print(json.dumps({"cells": args.cells, "sites": H.shape[0], "moments": args.moments, "launches": nl,
+                      "ms": ms, "bytes_per_launch": b, "GBps": b * nl / (ms / 1e3) / 1e9, "mu0": mu[0]}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,7 +379,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=64)
     ap.add_argument("--fp64-moments", type=int, default=256)
+    ap.add_argument("--kernel-only", action="store_true", help="small profiling case (no e2e/fp64/cpu legs)")
+    ap.add_argument("--cells", type=int, default=512)
+    ap.add_argument("--moments", type=int, default=32)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     args = ap.parse_args()
+    if args.kernel_only:
+        return run_kernel_only(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

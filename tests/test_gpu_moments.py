@@ -138,7 +138,7 @@ def test_resident_plan_is_deterministic_and_random_kets(gpu):
     f = tb.KpmSolver(G.scaled_HE, 16, precision="fp64", doubling=True)
     assert _err(f.run_random(128, 5), ref) <= 1e-10
     ms, launches, bytes_ = s.last_timing()
-    assert launches == 64 and ms > 0 and bytes_ > 0
+    assert launches == 65 and ms > 0 and bytes_ > 0
 
 
 def test_errors(gpu):

@@ -112,16 +112,18 @@ template <typename F> struct VecW { static constexpr int max_vpl = (sizeof(F) ==
 constexpr int kStepThreads = 256;
 constexpr int kStepWarps = kStepThreads / 32;
 
-// One recursion step over all rows.
-//   FIRST: y = H x                    else: y = 2 H x - y (y holds v_{n-1})
-//   BRAS == nullptr (doubling):   part[0] += <x|x>,  part[1] += <x|y>
-//   BRAS != nullptr (braket):     part[0] += <b|y>;  FIRST also part[1] += <b|x>
+// One recursion step over all rows, x = v_s, y = v_{s-1} on entry.
+//   FIRST: y = H x                    else: y = 2 H x - y  (v_{s+1} over v_{s-1})
+//   doubling (BRAKET false): part[0] += <x|x>; part[1] += <x|y_in> (= <v_s|v_{s-1}>),
+//                            FIRST: part[1] += <x|H x> (= <v_0|v_1>)
+//   braket:                  part[0] += <b|v_{s+1}>;  FIRST also part[1] += <b|x>
+//   gather == 0: no product at all (the last doubling step only needs the dots).
 template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET>
 __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     int32_t n, int32_t n_tiles, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
     const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
     typename C2<F>::T* y, const typename C2<F>::T* __restrict__ bras, double* __restrict__ part,
-    int store, int reverse) {
+    int store, int reverse, int gather) {
   using CT = typename C2<F>::T;
   constexpr int VPL = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
   constexpr int LPR = R / VPL;             // lanes per row
@@ -145,28 +147,30 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     LaneV<F, VPL> acc;
 #pragma unroll
     for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
-    HVal<F, CPLX_H>::load(diag, r).template fma<VPL>(xs, acc);
-    const int32_t s = r >> 5, l = r & 31;
-    const int32_t off = soff[s];
-    const int32_t w = (soff[s + 1] - off) >> 5;
-    const int32_t* cp = ecol + off + l;
-    int k = 0;
-    for (; k + 4 <= w; k += 4) {
-      int32_t c[4];
-      HVal<F, CPLX_H> h[4];
+    if (gather) {
+      HVal<F, CPLX_H>::load(diag, r).template fma<VPL>(xs, acc);
+      const int32_t s = r >> 5, l = r & 31;
+      const int32_t off = soff[s];
+      const int32_t w = (soff[s + 1] - off) >> 5;
+      const int32_t* cp = ecol + off + l;
+      int k = 0;
+      for (; k + 4 <= w; k += 4) {
+        int32_t c[4];
+        HVal<F, CPLX_H> h[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) { c[u] = __ldg(cp + (k + u) * 32); h[u] = HVal<F, CPLX_H>::load(eval, off + l + (int64_t)(k + u) * 32); }
-      LaneV<F, VPL> xv[4];
+        for (int u = 0; u < 4; ++u) { c[u] = __ldg(cp + (k + u) * 32); h[u] = HVal<F, CPLX_H>::load(eval, off + l + (int64_t)(k + u) * 32); }
+        LaneV<F, VPL> xv[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) xv[u] = ld_ro<F, VPL>(x + ((int64_t)c[u] * LPR + sub) * VPL);
+        for (int u = 0; u < 4; ++u) xv[u] = ld_ro<F, VPL>(x + ((int64_t)c[u] * LPR + sub) * VPL);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
-    }
-    for (; k < w; ++k) {
-      int32_t c = __ldg(cp + k * 32);
-      HVal<F, CPLX_H> h = HVal<F, CPLX_H>::load(eval, off + l + (int64_t)k * 32);
-      LaneV<F, VPL> xv = ld_ro<F, VPL>(x + ((int64_t)c * LPR + sub) * VPL);
-      h.template fma<VPL>(xv, acc);
+        for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
+      }
+      for (; k < w; ++k) {
+        int32_t c = __ldg(cp + k * 32);
+        HVal<F, CPLX_H> h = HVal<F, CPLX_H>::load(eval, off + l + (int64_t)k * 32);
+        LaneV<F, VPL> xv = ld_ro<F, VPL>(x + ((int64_t)c * LPR + sub) * VPL);
+        h.template fma<VPL>(xv, acc);
+      }
     }
     LaneV<F, VPL> out;
 #pragma unroll
@@ -174,7 +178,7 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
       if constexpr (FIRST) { out.re[q] = acc.re[q]; out.im[q] = acc.im[q]; }
       else { out.re[q] = F(2) * acc.re[q] - prev.re[q]; out.im[q] = F(2) * acc.im[q] - prev.im[q]; }
     }
-    if (store) st_v<F, VPL>(y + me * VPL, out);
+    // moment partial sums (before the store, from registers only)
     if constexpr (BRAKET) {
       const LaneV<F, VPL> b = ld_ro<F, VPL>(bras + me * VPL);
 #pragma unroll
@@ -186,9 +190,11 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
 #pragma unroll
       for (int q = 0; q < VPL; ++q) {
         m0 += xs.re[q] * xs.re[q] + xs.im[q] * xs.im[q];
-        m1 += xs.re[q] * out.re[q] + xs.im[q] * out.im[q];
+        if constexpr (FIRST) m1 += xs.re[q] * out.re[q] + xs.im[q] * out.im[q];
+        else m1 += xs.re[q] * prev.re[q] + xs.im[q] * prev.im[q];
       }
     }
+    if (store) st_v<F, VPL>(y + me * VPL, out);
   }
   // FP64 from here on: warp shuffle, then across the CTA's warps
   double d0 = (double)m0, d1 = (double)m1;
@@ -284,11 +290,12 @@ __global__ void assemble_moments_kernel(const double* __restrict__ sums, int32_t
   int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n_mom) return;
   if (doubling) {
+    // step s holds <v_s|v_s> (slot 0) and <v_s|v_{s-1}> (slot 1); step 0 holds mu_0, mu_1
     const double mu0 = sums[0], mu1 = sums[1];
-    int32_t s = k >> 1;
     if (k == 0) mu[k] = mu0;
     else if (k == 1) mu[k] = mu1;
-    else mu[k] = (k & 1) ? 2.0 * sums[2 * s + 1] - mu1 : 2.0 * sums[2 * s] - mu0;
+    else if (k & 1) mu[k] = 2.0 * sums[2 * ((k + 1) >> 1) + 1] - mu1;   // mu_2s-1, s = (k+1)/2
+    else mu[k] = 2.0 * sums[2 * (k >> 1)] - mu0;                         // mu_2s,   s = k/2
   } else {
     // step 0 holds <b|v1> in slot 0 and <b|v0> in slot 1; step s>0 holds <b|v_{s+1}>
     if (k == 0) mu[k] = sums[1];
@@ -307,7 +314,7 @@ struct StepArgs {
   void* y;
   const void* bras;
   double* part;
-  int store, reverse;
+  int store, reverse, gather;
 };
 
 template <typename F, int R, bool CPLX_H>
@@ -320,7 +327,7 @@ static int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
   auto dg = static_cast<const F*>(a.diag);
 #define TBK_STEP(FI, BR)                                                                   \
   kpm_step_kernel<F, R, CPLX_H, FI, BR><<<grid, kStepThreads, 0, st>>>(                    \
-      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, b, a.part, a.store, a.reverse)
+      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, b, a.part, a.store, a.reverse, a.gather)
   if (first) { if (braket) TBK_STEP(true, true); else TBK_STEP(true, false); }
   else { if (braket) TBK_STEP(false, true); else TBK_STEP(false, false); }
 #undef TBK_STEP
@@ -394,7 +401,8 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
                         double* mu_out, bool mu_device, cudaStream_t st) {
   if (n_mom < 2) return fail(TBK_ERR_INVALID, "n must be greater than or equal to 2");
   const bool doubling = !braket;
-  const int32_t n_steps = doubling ? (n_mom + 1) / 2 : n_mom - 1;
+  // doubling: step s yields mu_2s and mu_2s-1, so steps 0 .. n_mom/2 are needed
+  const int32_t n_steps = doubling ? (n_mom <= 2 ? 1 : n_mom / 2 + 1) : n_mom - 1;
   TBK_TRY(plan_partials(P, n_steps));
   TBK_TRY(plan_mu(P, n_mom));
   if (braket && P->bras.bytes < P->va.bytes) TBK_TRY(P->bras.alloc(P->va.bytes));
@@ -422,7 +430,9 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
       a.y = y;
       a.bras = braket ? P->bras.p : nullptr;
       a.part = P->part.as<double>() + (((int64_t)ch * n_steps + s) * 2) * P->grid;
-      a.store = (doubling && s == n_steps - 1) ? 0 : 1;
+      const bool last_dot = doubling && s == n_steps - 1 && s > 0;   // dots only, no product
+      a.store = last_dot ? 0 : 1;
+      a.gather = last_dot ? 0 : 1;
       a.reverse = (P->flags & TBK_FLAG_NO_L2_ZIGZAG) ? 0 : (s & 1);
       const bool first = s == 0;
       int rc;
@@ -455,11 +465,12 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
   const double mat = (double)E.n_entries * (4.0 + hv) + (double)E.n_rows * hv + 4.0 * (E.n_slices + 1);
   double per_chunk = 0.0;
   for (int32_t s = 0; s < n_steps; ++s) {
+    const bool last_dot = doubling && s == n_steps - 1 && s > 0;
     double b = vec;                                        // x
     if (s > 0) b += vec;                                   // v_{n-1}
-    if (!(doubling && s == n_steps - 1)) b += vec;         // y store
+    if (!last_dot) b += vec + mat;                         // y store + H~
     if (braket) b += vec;                                  // bras
-    per_chunk += b + mat;
+    per_chunk += b;
   }
   P->last_ms = ms_total;
   P->last_launches = launches;
