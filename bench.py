@@ -362,11 +362,14 @@ def run_kernel_only(args):
     X.set_scalar_disorder(W_DIS, 1)
     H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], float)
     G = tb.GreenFunction(args.moments, H, -BOUND, BOUND)
-    s = tb.KpmSolver(G.scaled_HE, R_VEC, precision=args.precision, doubling=args.precision == "mixed")
+    from tight_binding_gb300 import capi
+
+    flags = capi.FLAG_NO_TMA if args.no_tma else 0
+    s = tb.KpmSolver(G.scaled_HE, R_VEC, precision=args.precision, doubling=args.precision == "mixed", flags=flags)
     for _ in range(2):
         mu = s.run_random(args.moments, 0)
     ms, nl, b = s.last_timing()
-    print(json.dumps({"cells": args.cells, "sites": H.shape[0], "moments": args.moments, "launches": nl,
+    print(json.dumps({"tma": not args.no_tma, "precision": args.precision, "cells": args.cells, "sites": H.shape[0], "moments": args.moments, "launches": nl,
                       "ms": ms, "bytes_per_launch": b, "GBps": b * nl / (ms / 1e3) / 1e9, "mu0": mu[0]}))
     return 0
 
@@ -383,6 +386,7 @@ def main():
     ap.add_argument("--cells", type=int, default=512)
     ap.add_argument("--moments", type=int, default=32)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-tma", action="store_true", help="one-pass kernel without TMA staging (A/B)")
     args = ap.parse_args()
     if args.kernel_only:
         return run_kernel_only(args)

@@ -75,12 +75,26 @@ __device__ __forceinline__ void st_v(typename C2<F>::T* p, const LaneV<F, VPL>& 
   }
 }
 
+template <typename F, int VPL>
+__device__ __forceinline__ LaneV<F, VPL> ld_smem(const typename C2<F>::T* p) {
+  LaneV<F, VPL> o;
+  if constexpr (sizeof(F) == 4 && VPL == 2) {
+    float4 q = *reinterpret_cast<const float4*>(p);
+    o.re[0] = q.x; o.im[0] = q.y; o.re[1] = q.z; o.im[1] = q.w;
+  } else {
+    auto q = *p;
+    o.re[0] = q.x; o.im[0] = q.y;
+  }
+  return o;
+}
+
 template <typename F, bool CPLX_H>
 struct HVal;
 template <typename F>
 struct HVal<F, false> {
   F v;
   __device__ __forceinline__ static HVal load(const F* p, int64_t o) { return HVal{__ldg(p + o)}; }
+  __device__ __forceinline__ static HVal load_smem(const F* p, int32_t o) { return HVal{p[o]}; }
   template <int VPL>
   __device__ __forceinline__ void fma(const LaneV<F, VPL>& x, LaneV<F, VPL>& acc) const {
 #pragma unroll
@@ -93,6 +107,10 @@ struct HVal<F, true> {
   F r, i;
   __device__ __forceinline__ static HVal load(const F* p, int64_t o) {
     auto q = __ldg(reinterpret_cast<const typename C2<F>::T*>(p) + o);
+    return HVal{q.x, q.y};
+  }
+  __device__ __forceinline__ static HVal load_smem(const F* p, int32_t o) {
+    auto q = reinterpret_cast<const typename C2<F>::T*>(p)[o];
     return HVal{q.x, q.y};
   }
   template <int VPL>
@@ -215,6 +233,10 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
   }
 }
 
+}  // namespace tbk
+#include "kpm_tma.cuh"
+namespace tbk {
+
 // Column-major complex128 (Eigen) -> site-major work block of width Rp.
 template <typename F>
 __global__ void load_block_kernel(int32_t n, int32_t R, int32_t r0, int32_t rc, int32_t Rp,
@@ -305,7 +327,8 @@ __global__ void assemble_moments_kernel(const double* __restrict__ sums, int32_t
 
 // ----------------------------------------------------------------- dispatch
 struct StepArgs {
-  int32_t n, n_tiles;
+  int32_t n, n_tiles, n_slices;
+  int* err;
   const int32_t* soff;
   const int32_t* ecol;
   const void* eval;
@@ -351,6 +374,67 @@ static int launch_step(int R, const StepArgs& a, bool first, bool braket, int gr
   return fail(TBK_ERR_UNSUPPORTED, "chunk width %d not instantiated", R);
 }
 
+
+constexpr int kTmaStages = 4;
+
+template <typename F, int R, bool CPLX_H, bool BRAKET>
+static int tma_kernel_setup(int smem, int* occ) {
+  auto kern = kpm_tma_step_kernel<F, R, CPLX_H, BRAKET, kTmaStages>;
+  TBK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int nb = 0;
+  TBK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kTmaThreads, smem));
+  *occ = nb;
+  return TBK_OK;
+}
+
+template <typename F, int R, bool CPLX_H>
+static int launch_tma_r(const StepArgs& a, const TmaLayout& L, bool first, bool braket, int grid, cudaStream_t st) {
+  using CT = typename C2<F>::T;
+  const int smem = L.stage_bytes * kTmaStages;
+  auto x = static_cast<const CT*>(a.x);
+  auto y = static_cast<CT*>(a.y);
+  auto b = static_cast<const CT*>(a.bras);
+  auto ev = static_cast<const F*>(a.eval);
+  auto dg = static_cast<const F*>(a.diag);
+  if (braket)
+    kpm_tma_step_kernel<F, R, CPLX_H, true, kTmaStages><<<grid, kTmaThreads, smem, st>>>(
+        a.n, a.n_slices, a.n_tiles, L, a.soff, a.ecol, ev, dg, x, y, b, a.part, a.store, a.reverse, a.gather,
+        first ? 1 : 0, a.err);
+  else
+    kpm_tma_step_kernel<F, R, CPLX_H, false, kTmaStages><<<grid, kTmaThreads, smem, st>>>(
+        a.n, a.n_slices, a.n_tiles, L, a.soff, a.ecol, ev, dg, x, y, b, a.part, a.store, a.reverse, a.gather,
+        first ? 1 : 0, a.err);
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
+}
+
+#define TBK_R_SWITCH(R, CALL64, CALL)                                   \
+  switch (R) {                                                          \
+    case 1: CALL(1); case 2: CALL(2); case 4: CALL(4); case 8: CALL(8);   \
+    case 16: CALL(16); case 32: CALL(32); case 64: CALL64(64);          \
+  }
+
+template <typename F, bool CPLX_H>
+static int launch_tma(int R, const StepArgs& a, const TmaLayout& L, bool first, bool braket, int grid,
+                      cudaStream_t st) {
+#define TBK_CALL(RR) return launch_tma_r<F, RR, CPLX_H>(a, L, first, braket, grid, st)
+#define TBK_CALL64(RR) if constexpr (sizeof(F) == 4) { TBK_CALL(RR); } break
+  TBK_R_SWITCH(R, TBK_CALL64, TBK_CALL)
+#undef TBK_CALL
+#undef TBK_CALL64
+  return fail(TBK_ERR_UNSUPPORTED, "chunk width %d not instantiated", R);
+}
+
+template <typename F, bool CPLX_H>
+static int tma_setup(int R, bool braket, int smem, int* occ) {
+#define TBK_CALL(RR) return braket ? tma_kernel_setup<F, RR, CPLX_H, true>(smem, occ) : tma_kernel_setup<F, RR, CPLX_H, false>(smem, occ)
+#define TBK_CALL64(RR) if constexpr (sizeof(F) == 4) { TBK_CALL(RR); } break
+  TBK_R_SWITCH(R, TBK_CALL64, TBK_CALL)
+#undef TBK_CALL
+#undef TBK_CALL64
+  return fail(TBK_ERR_UNSUPPORTED, "chunk width %d not instantiated", R);
+}
+
 template <typename F, bool CPLX_H, int R>
 static int occupancy_blocks() {
   int nb = 0;
@@ -373,8 +457,13 @@ struct tbk_kpm_s {
   int32_t R = 0, Rc = 0, n_chunks = 0, flags = 0, prec = 0;
   int64_t n = 0;
   size_t csize = 0;                 // bytes of one complex element
-  DevBuf va, vb, bras, stage, part, sums, mu;
-  int grid = 0, n_tiles = 0;
+  DevBuf va, vb, bras, stage, part, sums, mu, err;
+  int grid = 0, n_tiles = 0;        // legacy (one row group per warp) kernel
+  int64_t n_pad = 0;                // rows of the work blocks (whole 32-row slices)
+  bool use_tma = false;             // TMA-staged warp-specialised kernel
+  TmaLayout lay_dbl{}, lay_brk{};   // stage layouts: doubling / braket
+  int grid_dbl = 0, grid_brk = 0, tiles_tma = 0;
+  int grid_max = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0, last_bytes = 0.0;
   int32_t last_launches = 0;
@@ -383,7 +472,7 @@ struct tbk_kpm_s {
 
 static int plan_partials(tbk_kpm_s* P, int32_t n_steps) {
   if (n_steps <= P->cap_steps) return TBK_OK;
-  TBK_TRY(P->part.alloc(sizeof(double) * 2 * (size_t)n_steps * P->grid * P->n_chunks));
+  TBK_TRY(P->part.alloc(sizeof(double) * 2 * (size_t)n_steps * P->grid_max * P->n_chunks));
   TBK_TRY(P->sums.alloc(sizeof(double) * 2 * (size_t)n_steps));
   P->cap_steps = n_steps;
   return TBK_OK;
@@ -405,8 +494,15 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
   const int32_t n_steps = doubling ? (n_mom <= 2 ? 1 : n_mom / 2 + 1) : n_mom - 1;
   TBK_TRY(plan_partials(P, n_steps));
   TBK_TRY(plan_mu(P, n_mom));
-  if (braket && P->bras.bytes < P->va.bytes) TBK_TRY(P->bras.alloc(P->va.bytes));
+  if (braket && P->bras.bytes < P->va.bytes) {
+    TBK_TRY(P->bras.alloc(P->va.bytes));
+    TBK_CUDA(cudaMemsetAsync(P->bras.p, 0, P->bras.bytes, st));
+  }
   const EllDev& E = P->H->ell;
+  const bool tma = P->use_tma && !(P->flags & TBK_FLAG_NO_TMA);
+  const int G = tma ? (braket ? P->grid_brk : P->grid_dbl) : P->grid;
+  const TmaLayout& lay = braket ? P->lay_brk : P->lay_dbl;
+  TBK_CUDA(cudaMemsetAsync(P->err.p, 0, sizeof(int), st));
   const bool mixed = P->prec == TBK_PREC_MIXED;
   const bool cplx = P->H->is_complex != 0;
   float ms_total = 0.f;
@@ -421,7 +517,9 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
     for (int32_t s = 0; s < n_steps; ++s) {
       StepArgs a;
       a.n = (int32_t)P->n;
-      a.n_tiles = P->n_tiles;
+      a.n_tiles = tma ? P->tiles_tma : P->n_tiles;
+      a.n_slices = E.n_slices;
+      a.err = P->err.as<int>();
       a.soff = E.slice_off.as<int32_t>();
       a.ecol = E.col.as<int32_t>();
       a.eval = mixed ? E.val32.p : E.val64.p;
@@ -429,17 +527,24 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
       a.x = x;
       a.y = y;
       a.bras = braket ? P->bras.p : nullptr;
-      a.part = P->part.as<double>() + (((int64_t)ch * n_steps + s) * 2) * P->grid;
+      a.part = P->part.as<double>() + (((int64_t)ch * n_steps + s) * 2) * G;
       const bool last_dot = doubling && s == n_steps - 1 && s > 0;   // dots only, no product
       a.store = last_dot ? 0 : 1;
       a.gather = last_dot ? 0 : 1;
       a.reverse = (P->flags & TBK_FLAG_NO_L2_ZIGZAG) ? 0 : (s & 1);
       const bool first = s == 0;
       int rc;
-      if (mixed) rc = cplx ? launch_step<float, true>(P->Rc, a, first, braket, P->grid, st)
-                           : launch_step<float, false>(P->Rc, a, first, braket, P->grid, st);
-      else rc = cplx ? launch_step<double, true>(P->Rc, a, first, braket, P->grid, st)
-                     : launch_step<double, false>(P->Rc, a, first, braket, P->grid, st);
+      if (tma) {
+        if (mixed) rc = cplx ? launch_tma<float, true>(P->Rc, a, lay, first, braket, G, st)
+                             : launch_tma<float, false>(P->Rc, a, lay, first, braket, G, st);
+        else rc = cplx ? launch_tma<double, true>(P->Rc, a, lay, first, braket, G, st)
+                       : launch_tma<double, false>(P->Rc, a, lay, first, braket, G, st);
+      } else {
+        if (mixed) rc = cplx ? launch_step<float, true>(P->Rc, a, first, braket, G, st)
+                             : launch_step<float, false>(P->Rc, a, first, braket, G, st);
+        else rc = cplx ? launch_step<double, true>(P->Rc, a, first, braket, G, st)
+                       : launch_step<double, false>(P->Rc, a, first, braket, G, st);
+      }
       if (rc != TBK_OK) return rc;
       ++launches;
       std::swap(x, y);   // y now holds v_{n+1}; it becomes x, x (v_n) becomes the next v_{n-1}
@@ -450,7 +555,7 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
     TBK_CUDA(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
     ms_total += ms;
   }
-  reduce_partials_kernel<<<dim3(n_steps, 2), 256, 0, st>>>(P->part.as<double>(), P->n_chunks, n_steps, P->grid,
+  reduce_partials_kernel<<<dim3(n_steps, 2), 256, 0, st>>>(P->part.as<double>(), P->n_chunks, n_steps, G,
                                                           P->sums.as<double>());
   TBK_CHECK_LAUNCH();
   assemble_moments_kernel<<<(n_mom + 255) / 256, 256, 0, st>>>(P->sums.as<double>(), n_mom, doubling ? 1 : 0,
@@ -458,7 +563,10 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
   TBK_CHECK_LAUNCH();
   if (mu_device) TBK_CUDA(cudaMemcpyAsync(mu_out, P->mu.p, sizeof(double) * n_mom, cudaMemcpyDeviceToDevice, st));
   else TBK_CUDA(cudaMemcpyAsync(mu_out, P->mu.p, sizeof(double) * n_mom, cudaMemcpyDeviceToHost, st));
+  int herr = 0;
+  TBK_CUDA(cudaMemcpyAsync(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
   TBK_CUDA(cudaStreamSynchronize(st));
+  if (herr) return fail(TBK_ERR_TIMEOUT, "recursion kernel gave up waiting (code %d)", herr);
   // algorithmic DRAM bytes per recursion launch (average over the launches)
   const double vec = (double)P->n * P->Rc * P->csize;
   const double hv = (mixed ? 4.0 : 8.0) * (cplx ? 2.0 : 1.0);
@@ -517,9 +625,50 @@ int tbk_kpm_create(tbk_kpm* out, tbk_sparse Ht, int32_t R, int32_t flags) {
   else { if (cplx) { OCC(double, true) } else { OCC(double, false) } }
 #undef OCC
   P->grid = std::max(1, std::min(P->n_tiles, sm_count() * occ));
-  const size_t blk = (size_t)P->n * rc * P->csize;
+  P->grid_max = P->grid;
+  P->n_pad = (int64_t)Ht->ell.n_slices * 32;
+  // TMA-staged kernel: tiles of whole slices, ~8 KB of vector rows per stream
+  {
+    const int row_bytes = rc * (int)P->csize;
+    int TR = 8192 / row_bytes;
+    TR = std::max(32, std::min(512, TR)) & ~31;
+    const int hsize = (prec == TBK_PREC_MIXED ? 4 : 8) * (cplx ? 2 : 1);
+    const int wmax = std::max(1, Ht->ell.max_width);
+    P->lay_dbl = make_tma_layout(TR, wmax, rc, (int)P->csize, hsize, false);
+    P->lay_brk = make_tma_layout(TR, wmax, rc, (int)P->csize, hsize, true);
+    const int smem_brk = P->lay_brk.stage_bytes * kTmaStages;
+    // FP64 on GB300 is bound by the FP64 pipe, where more resident warps of the
+    // one-pass kernel beat the staged ring; the staged kernel serves complex64.
+    if (prec == TBK_PREC_MIXED && smem_brk <= 200 * 1024 && Ht->ell.n_slices > 0) {
+      int occ_d = 0, occ_b = 0, st1, st2;
+      if (prec == TBK_PREC_MIXED) {
+        st1 = cplx ? tma_setup<float, true>(rc, false, P->lay_dbl.stage_bytes * kTmaStages, &occ_d)
+                   : tma_setup<float, false>(rc, false, P->lay_dbl.stage_bytes * kTmaStages, &occ_d);
+        st2 = cplx ? tma_setup<float, true>(rc, true, smem_brk, &occ_b) : tma_setup<float, false>(rc, true, smem_brk, &occ_b);
+      } else {
+        st1 = cplx ? tma_setup<double, true>(rc, false, P->lay_dbl.stage_bytes * kTmaStages, &occ_d)
+                   : tma_setup<double, false>(rc, false, P->lay_dbl.stage_bytes * kTmaStages, &occ_d);
+        st2 = cplx ? tma_setup<double, true>(rc, true, smem_brk, &occ_b) : tma_setup<double, false>(rc, true, smem_brk, &occ_b);
+      }
+      if (st1 == TBK_OK && st2 == TBK_OK && occ_d > 0 && occ_b > 0) {
+        P->tiles_tma = (int)((P->n_pad + TR - 1) / TR);
+        P->grid_dbl = std::max(1, std::min(P->tiles_tma, sm_count() * occ_d));
+        P->grid_brk = std::max(1, std::min(P->tiles_tma, sm_count() * occ_b));
+        P->grid_max = std::max(P->grid_max, std::max(P->grid_dbl, P->grid_brk));
+        P->use_tma = true;
+      }
+    }
+  }
+  const size_t blk = (size_t)P->n_pad * rc * P->csize;
   int s;
-  if ((s = P->va.alloc(blk)) != TBK_OK || (s = P->vb.alloc(blk)) != TBK_OK) { delete P; return s; }
+  if ((s = P->va.alloc(blk)) != TBK_OK || (s = P->vb.alloc(blk)) != TBK_OK || (s = P->err.alloc(sizeof(int))) != TBK_OK) {
+    delete P;
+    return s;
+  }
+  if (cudaMemset(P->va.p, 0, blk) != cudaSuccess || cudaMemset(P->vb.p, 0, blk) != cudaSuccess) {
+    delete P;
+    return fail(TBK_ERR_CUDA, "cudaMemset of the work blocks failed");
+  }
   if (cudaEventCreate(&P->ev0) != cudaSuccess || cudaEventCreate(&P->ev1) != cudaSuccess) {
     delete P;
     return fail(TBK_ERR_CUDA, "cudaEventCreate failed");
