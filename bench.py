@@ -364,12 +364,12 @@ def run_kernel_only(args):
     G = tb.GreenFunction(args.moments, H, -BOUND, BOUND)
     from tight_binding_gb300 import capi
 
-    flags = capi.FLAG_NO_TMA if args.no_tma else 0
+    flags = capi.FLAG_STAGED if args.staged else 0
     s = tb.KpmSolver(G.scaled_HE, R_VEC, precision=args.precision, doubling=args.precision == "mixed", flags=flags)
     for _ in range(2):
         mu = s.run_random(args.moments, 0)
     ms, nl, b = s.last_timing()
-    print(json.dumps({"tma": not args.no_tma, "precision": args.precision, "cells": args.cells, "sites": H.shape[0], "moments": args.moments, "launches": nl,
+    print(json.dumps({"staged": args.staged, "precision": args.precision, "cells": args.cells, "sites": H.shape[0], "moments": args.moments, "launches": nl,
                       "ms": ms, "bytes_per_launch": b, "GBps": b * nl / (ms / 1e3) / 1e9, "mu0": mu[0]}))
     return 0
 
@@ -386,7 +386,7 @@ def main():
     ap.add_argument("--cells", type=int, default=512)
     ap.add_argument("--moments", type=int, default=32)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--no-tma", action="store_true", help="one-pass kernel without TMA staging (A/B)")
+    ap.add_argument("--staged", action="store_true", help="TMA-staged warp-specialised kernel (A/B)")
     args = ap.parse_args()
     if args.kernel_only:
         return run_kernel_only(args)

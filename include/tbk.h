@@ -55,7 +55,7 @@ enum {
                                      <v_n+1|v_n> — half the recursion steps      */
   TBK_FLAG_DEVICE_PTRS = 1 << 5,  /* bras/kets/mu are device pointers           */
   TBK_FLAG_NO_L2_ZIGZAG = 1 << 6, /* keep every step's sweep ascending          */
-  TBK_FLAG_NO_TMA = 1 << 7        /* use the one-pass kernel without TMA staging */
+  TBK_FLAG_STAGED = 1 << 7        /* TMA-staged warp-specialised step kernel      */
 };
 
 /* =========================================================================

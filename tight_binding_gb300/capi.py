@@ -27,7 +27,7 @@ PREC_MIXED = 1
 FLAG_DOUBLING = 1 << 4
 FLAG_DEVICE_PTRS = 1 << 5
 FLAG_NO_L2_ZIGZAG = 1 << 6
-FLAG_NO_TMA = 1 << 7
+FLAG_STAGED = 1 << 7
 
 BUILD_SPARSE = 0
 BUILD_PERIODIC_BARE = 1

@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <vector>
 
@@ -95,6 +96,7 @@ struct HVal<F, false> {
   F v;
   __device__ __forceinline__ static HVal load(const F* p, int64_t o) { return HVal{__ldg(p + o)}; }
   __device__ __forceinline__ static HVal load_smem(const F* p, int32_t o) { return HVal{p[o]}; }
+  __device__ __forceinline__ static HVal zero() { return HVal{F(0)}; }
   template <int VPL>
   __device__ __forceinline__ void fma(const LaneV<F, VPL>& x, LaneV<F, VPL>& acc) const {
 #pragma unroll
@@ -113,6 +115,7 @@ struct HVal<F, true> {
     auto q = reinterpret_cast<const typename C2<F>::T*>(p)[o];
     return HVal{q.x, q.y};
   }
+  __device__ __forceinline__ static HVal zero() { return HVal{F(0), F(0)}; }
   template <int VPL>
   __device__ __forceinline__ void fma(const LaneV<F, VPL>& x, LaneV<F, VPL>& acc) const {
 #pragma unroll
@@ -126,6 +129,12 @@ struct HVal<F, true> {
 };
 
 template <typename F> struct VecW { static constexpr int max_vpl = (sizeof(F) == 4) ? 2 : 1; };
+
+// Asynchronous bulk prefetch of [src, src+bytes) into L2 (no shared memory, no
+// completion to wait for); bytes % 16 == 0 and src 16-byte aligned.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 
 constexpr int kStepThreads = 256;
 constexpr int kStepWarps = kStepThreads / 32;
@@ -141,7 +150,7 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     int32_t n, int32_t n_tiles, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
     const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
     typename C2<F>::T* y, const typename C2<F>::T* __restrict__ bras, double* __restrict__ part,
-    int store, int reverse, int gather) {
+    int store, int reverse, int gather, int pf_dist) {
   using CT = typename C2<F>::T;
   constexpr int VPL = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
   constexpr int LPR = R / VPL;             // lanes per row
@@ -156,6 +165,24 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
 
   for (int32_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     const int32_t tile = reverse ? (n_tiles - 1 - t) : t;
+    if (pf_dist > 0 && threadIdx.x == 0) {
+      // bring the streams of the tile this CTA reaches pf_dist iterations later
+      // into L2 ahead of time: its own rows of v_n and v_{n-1} (and the bras)
+      const int32_t tf = t + pf_dist * (int32_t)gridDim.x;
+      if (tf < n_tiles) {
+        const int32_t tilef = reverse ? (n_tiles - 1 - tf) : tf;
+        const int64_t rf = (int64_t)tilef * ROWS_PER_TILE;
+        const int32_t nr = (int32_t)min((int64_t)ROWS_PER_TILE, (int64_t)n - rf);
+        if (nr > 0) {
+          const uint32_t vb = (uint32_t)nr * (uint32_t)(R * sizeof(CT));
+          if ((vb & 15u) == 0) {
+            bulk_prefetch_l2(x + rf * R, vb);
+            if (!FIRST) bulk_prefetch_l2(y + rf * R, vb);
+            if (BRAKET) bulk_prefetch_l2(bras + rf * R, vb);
+          }
+        }
+      }
+    }
     const int32_t r = tile * ROWS_PER_TILE + warp * RPW + lane / LPR;
     if (r >= n) continue;
     const int64_t me = (int64_t)r * LPR + sub;
@@ -171,23 +198,21 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
       const int32_t off = soff[s];
       const int32_t w = (soff[s + 1] - off) >> 5;
       const int32_t* cp = ecol + off + l;
-      int k = 0;
-      for (; k + 4 <= w; k += 4) {
+      // all of a row's gathers in flight together: predicated groups of 4
+      for (int k = 0; k < w; k += 4) {
         int32_t c[4];
         HVal<F, CPLX_H> h[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) { c[u] = __ldg(cp + (k + u) * 32); h[u] = HVal<F, CPLX_H>::load(eval, off + l + (int64_t)(k + u) * 32); }
+        for (int u = 0; u < 4; ++u) {
+          const bool v = k + u < w;
+          c[u] = v ? __ldg(cp + (k + u) * 32) : r;                  // padding: own row
+          h[u] = v ? HVal<F, CPLX_H>::load(eval, off + l + (int64_t)(k + u) * 32) : HVal<F, CPLX_H>::zero();
+        }
         LaneV<F, VPL> xv[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) xv[u] = ld_ro<F, VPL>(x + ((int64_t)c[u] * LPR + sub) * VPL);
 #pragma unroll
         for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
-      }
-      for (; k < w; ++k) {
-        int32_t c = __ldg(cp + k * 32);
-        HVal<F, CPLX_H> h = HVal<F, CPLX_H>::load(eval, off + l + (int64_t)k * 32);
-        LaneV<F, VPL> xv = ld_ro<F, VPL>(x + ((int64_t)c * LPR + sub) * VPL);
-        h.template fma<VPL>(xv, acc);
       }
     }
     LaneV<F, VPL> out;
@@ -337,7 +362,7 @@ struct StepArgs {
   void* y;
   const void* bras;
   double* part;
-  int store, reverse, gather;
+  int store, reverse, gather, pf_dist;
 };
 
 template <typename F, int R, bool CPLX_H>
@@ -350,7 +375,7 @@ static int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
   auto dg = static_cast<const F*>(a.diag);
 #define TBK_STEP(FI, BR)                                                                   \
   kpm_step_kernel<F, R, CPLX_H, FI, BR><<<grid, kStepThreads, 0, st>>>(                    \
-      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, b, a.part, a.store, a.reverse, a.gather)
+      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, b, a.part, a.store, a.reverse, a.gather, a.pf_dist)
   if (first) { if (braket) TBK_STEP(true, true); else TBK_STEP(true, false); }
   else { if (braket) TBK_STEP(false, true); else TBK_STEP(false, false); }
 #undef TBK_STEP
@@ -464,6 +489,7 @@ struct tbk_kpm_s {
   TmaLayout lay_dbl{}, lay_brk{};   // stage layouts: doubling / braket
   int grid_dbl = 0, grid_brk = 0, tiles_tma = 0;
   int grid_max = 0;
+  int pf_dist = 1;                  // L2 prefetch distance of the one-pass kernel (grid-stride waves)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0, last_bytes = 0.0;
   int32_t last_launches = 0;
@@ -499,7 +525,7 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
     TBK_CUDA(cudaMemsetAsync(P->bras.p, 0, P->bras.bytes, st));
   }
   const EllDev& E = P->H->ell;
-  const bool tma = P->use_tma && !(P->flags & TBK_FLAG_NO_TMA);
+  const bool tma = P->use_tma && (P->flags & TBK_FLAG_STAGED);
   const int G = tma ? (braket ? P->grid_brk : P->grid_dbl) : P->grid;
   const TmaLayout& lay = braket ? P->lay_brk : P->lay_dbl;
   TBK_CUDA(cudaMemsetAsync(P->err.p, 0, sizeof(int), st));
@@ -520,6 +546,7 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
       a.n_tiles = tma ? P->tiles_tma : P->n_tiles;
       a.n_slices = E.n_slices;
       a.err = P->err.as<int>();
+      a.pf_dist = P->pf_dist;
       a.soff = E.slice_off.as<int32_t>();
       a.ecol = E.col.as<int32_t>();
       a.eval = mixed ? E.val32.p : E.val64.p;
@@ -626,11 +653,13 @@ int tbk_kpm_create(tbk_kpm* out, tbk_sparse Ht, int32_t R, int32_t flags) {
 #undef OCC
   P->grid = std::max(1, std::min(P->n_tiles, sm_count() * occ));
   P->grid_max = P->grid;
+  if (const char* e = getenv("TBK_PREFETCH")) P->pf_dist = atoi(e);   // tuning override
   P->n_pad = (int64_t)Ht->ell.n_slices * 32;
   // TMA-staged kernel: tiles of whole slices, ~8 KB of vector rows per stream
   {
     const int row_bytes = rc * (int)P->csize;
     int TR = 8192 / row_bytes;
+    if (const char* e = getenv("TBK_TMA_ROWS")) TR = atoi(e);   // tuning override (rows per tile)
     TR = std::max(32, std::min(512, TR)) & ~31;
     const int hsize = (prec == TBK_PREC_MIXED ? 4 : 8) * (cplx ? 2 : 1);
     const int wmax = std::max(1, Ht->ell.max_width);

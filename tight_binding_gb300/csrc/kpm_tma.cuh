@@ -63,6 +63,20 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
+// Same with an L2 cache policy (e.g. evict-first for data read exactly once).
+__device__ __forceinline__ void bulk_g2s_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                              uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
 
 // Shared-memory layout of one stage (byte offsets, all 128-byte aligned).
 struct TmaLayout {
@@ -138,6 +152,7 @@ __global__ void __launch_bounds__(kTmaThreads) kpm_tma_step_kernel(
     if (lane == 0) {
       int32_t issued = 0;
       bool ok = true;
+      const uint64_t once = policy_evict_first();   // v_{n-1}, bras and the ELL are read once
       for (int32_t k = 0; k < my_tiles; ++k) {
         const int st = k % STAGES;
         const uint32_t ph = (uint32_t)(k / STAGES) & 1u;
@@ -158,11 +173,11 @@ __global__ void __launch_bounds__(kTmaThreads) kpm_tma_step_kernel(
         unsigned char* sb = smem + (size_t)st * L.stage_bytes;
         mbar_arrive_expect_tx(&full_bar[st], bytes);
         bulk_g2s(sb + L.off_x, x + (size_t)r0 * R, vbytes, &full_bar[st]);
-        if (!first) bulk_g2s(sb + L.off_prev, y + (size_t)r0 * R, vbytes, &full_bar[st]);
-        if (BRAKET) bulk_g2s(sb + L.off_bras, bras + (size_t)r0 * R, vbytes, &full_bar[st]);
+        if (!first) bulk_g2s_hint(sb + L.off_prev, y + (size_t)r0 * R, vbytes, &full_bar[st], once);
+        if (BRAKET) bulk_g2s_hint(sb + L.off_bras, bras + (size_t)r0 * R, vbytes, &full_bar[st], once);
         if (gather && ell_n) {
-          bulk_g2s(sb + L.off_col, ecol + e0, ell_n * 4u, &full_bar[st]);
-          bulk_g2s(sb + L.off_val, eval + (size_t)e0 * HS, ell_n * (uint32_t)(sizeof(F) * HS), &full_bar[st]);
+          bulk_g2s_hint(sb + L.off_col, ecol + e0, ell_n * 4u, &full_bar[st], once);
+          bulk_g2s_hint(sb + L.off_val, eval + (size_t)e0 * HS, ell_n * (uint32_t)(sizeof(F) * HS), &full_bar[st], once);
         }
         bulk_g2s(sb + L.off_diag, diag + (size_t)r0 * HS, dbytes, &full_bar[st]);
         ++issued;
@@ -196,6 +211,13 @@ __global__ void __launch_bounds__(kTmaThreads) kpm_tma_step_kernel(
     const int32_t r0 = tile * L.TR;
     const int32_t s0 = tile * slices_per_tile;
     const int32_t e0 = __ldg(soff + s0);
+    const uint32_t tile_rows = (uint32_t)min(L.TR, n_slices * 32 - r0);   // rows staged in shared memory
+    // neighbour row c: from the staged tile when it lies inside it, else from global (L2)
+    auto nbr = [&](int32_t c) -> LaneV<F, VPL> {
+      const uint32_t lc = (uint32_t)(c - r0);
+      if (lc < tile_rows) return ld_smem<F, VPL>(sx + ((size_t)lc * LPR + sub) * VPL);
+      return ld_ro<F, VPL>(x + ((int64_t)c * LPR + sub) * VPL);
+    };
     for (int32_t lr = warp * RPW + lane / LPR; lr < L.TR; lr += ROWS_PER_PASS) {
       // rows past n (slice padding) are skipped; n <= padded rows of this tile
       const int32_t r = r0 + lr;
@@ -214,26 +236,22 @@ __global__ void __launch_bounds__(kTmaThreads) kpm_tma_step_kernel(
         const int32_t s = lr >> 5, l = lr & 31;
         const int32_t off = __ldg(soff + s0 + s) - e0;
         const int32_t w = (__ldg(soff + s0 + s + 1) - __ldg(soff + s0 + s)) >> 5;
-        int kk = 0;
-        for (; kk + 4 <= w; kk += 4) {
+        // all of a row's gathers in flight together: predicated groups of 4
+        for (int kk = 0; kk < w; kk += 4) {
           int32_t c[4];
           HVal<F, CPLX_H> h[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
-            c[u] = scol[off + (kk + u) * 32 + l];
-            h[u] = HVal<F, CPLX_H>::load_smem(sval, off + (kk + u) * 32 + l);
+            const bool v = kk + u < w;
+            c[u] = v ? scol[off + (kk + u) * 32 + l] : r;          // padding: own row (staged)
+            h[u] = HVal<F, CPLX_H>::load_smem(sval, v ? off + (kk + u) * 32 + l : off + l);
+            if (!v) h[u] = HVal<F, CPLX_H>::zero();
           }
           LaneV<F, VPL> xv[4];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) xv[u] = ld_ro<F, VPL>(x + ((int64_t)c[u] * LPR + sub) * VPL);
+          for (int u = 0; u < 4; ++u) xv[u] = nbr(c[u]);
 #pragma unroll
           for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
-        }
-        for (; kk < w; ++kk) {
-          const int32_t c = scol[off + kk * 32 + l];
-          HVal<F, CPLX_H> h = HVal<F, CPLX_H>::load_smem(sval, off + kk * 32 + l);
-          LaneV<F, VPL> xv = ld_ro<F, VPL>(x + ((int64_t)c * LPR + sub) * VPL);
-          h.template fma<VPL>(xv, acc);
         }
       }
       LaneV<F, VPL> out;
