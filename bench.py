@@ -358,7 +358,10 @@ def run_kernel_only(args):
     solve (doubling) on a honeycomb of --cells^2 cells, R = 32."""
     import tight_binding_gb300 as tb
 
-    X = tb.PartialLattice(tb.Honeycomb().add_hopping("A", 1, T_HOP), (args.cells, args.cells))
+    cell = tb.Honeycomb()
+    if not args.no_hopping:
+        cell.add_hopping("A", 1, T_HOP)
+    X = tb.PartialLattice(cell, (args.cells, args.cells))
     X.set_scalar_disorder(W_DIS, 1)
     H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], float)
     G = tb.GreenFunction(args.moments, H, -BOUND, BOUND)
@@ -369,7 +372,7 @@ def run_kernel_only(args):
     for _ in range(2):
         mu = s.run_random(args.moments, 0)
     ms, nl, b = s.last_timing()
-    print(json.dumps({"staged": args.staged, "precision": args.precision, "cells": args.cells, "sites": H.shape[0], "moments": args.moments, "launches": nl,
+    print(json.dumps({"staged": args.staged, "no_hopping": args.no_hopping, "precision": args.precision, "cells": args.cells, "sites": H.shape[0], "moments": args.moments, "launches": nl,
                       "ms": ms, "bytes_per_launch": b, "GBps": b * nl / (ms / 1e3) / 1e9, "mu0": mu[0]}))
     return 0
 
@@ -387,6 +390,8 @@ def main():
     ap.add_argument("--moments", type=int, default=32)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--staged", action="store_true", help="TMA-staged warp-specialised kernel (A/B)")
+    ap.add_argument("--no-hopping", action="store_true",
+                    help="diagonal-only H (same vector streams, no neighbour gathers): stream ceiling")
     args = ap.parse_args()
     if args.kernel_only:
         return run_kernel_only(args)
