@@ -215,6 +215,25 @@ int tbk_dos_from_moments(int32_t n, const double* mu, int32_t kernel_kind, doubl
                          double p1, double R, int32_t n_e, const double* e, double* rho,
                          void* stream);
 
+/* =========================================================================
+ * Chebyshev moments without device allocation.  No counterpart in the
+ * reference: it serves callers that may not allocate GPU memory while they run
+ * (a fixed, fully reserved HBM budget; a host that lends device buffers but
+ * forbids allocation; loops where cudaMalloc would synchronise the device).
+ * Same result as tbk_cheb_braket_* (FP64 recursion, plain braket moments) for
+ * a matrix given in device CSR form (row_ptr[n_rows+1], col_idx, values real or
+ * complex interleaved) and device bras/kets (N x R column-major complex128);
+ * mu_out is a device array of n_mom doubles, ready when `stream` completes.
+ * Work space is a fixed file-scope device array of 32.06 MiB: N * R must not
+ * exceed 1,048,576 (larger sizes fail with TBK_ERR_INVALID).  Calls share that
+ * array, so calls that overlap on the GPU race; the first call on a device
+ * looks up the array's address and should come before any stream capture.
+ * Nothing is allocated or freed. */
+int tbk_cheb_moments_noalloc(int32_t n_rows, const int32_t* row_ptr, const int32_t* col_idx,
+                             const double* values, int32_t is_complex, int32_t n_mom,
+                             const double* bras, const double* kets, int32_t R, double* mu_out,
+                             void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -83,6 +83,7 @@ SIGNATURES = {
     "tbk_green_imag_eval": (C.c_int, [_i32, _vp, _vp, _i32, _vp, _vp, _vp]),
     "tbk_green_imag_fft": (C.c_int, [_i32, _vp, _vp, _i32, _vp, _vp, _vp]),
     "tbk_dos_from_moments": (C.c_int, [_i32, _vp, _i32, _d, _d, _d, _i32, _vp, _vp, _vp]),
+    "tbk_cheb_moments_noalloc": (C.c_int, [_i32, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp]),
 }
 
 
