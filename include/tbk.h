@@ -216,6 +216,36 @@ int tbk_dos_from_moments(int32_t n, const double* mu, int32_t kernel_kind, doubl
                          void* stream);
 
 /* =========================================================================
+ * Kubo conductivities from double-Chebyshev moments.
+ * ========================================================================= */
+enum { TBK_MU_CUDA_CORE = 0, TBK_MU_TENSOR = 1 };
+/* mu_mn = sum_{sites,r} conj(aL_m) aR_n with aL_m = g_m AL T_m(H~) BL |r>,
+ * aR_n = g_n AR T_n(H~) BR |r> (NULL operator = identity), m, n < M: the stored
+ * Chebyshev blocks of TB/numerical.h:333-344 contracted as in TB/snippets.h:
+ * 337-342 (Bastin: AL=BL=1, AR=v_x, BR=v_y), :225-260 (Greenwood: AL=BL=v_x)
+ * and :491-518 (generate_V_moments).  Blocks are complex64 in HBM; R vectors
+ * are processed in chunks so both sides fit block_budget_gb (<= 0: 40 GB).
+ * kets: host N x R column-major complex128, or NULL for seeded random phases.
+ * kernel: TBK_KERNEL_* with parameters kp0/kp1 (g_m).  flags: TBK_MU_*.
+ * mu_out: host M x M complex128, row m = left index. */
+int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_sparse BR, int32_t M,
+                int32_t R, uint64_t seed, const double* kets, int32_t kernel_kind, double kp0,
+                double kp1, int32_t flags, double block_budget_gb, double* mu_out, void* stream);
+/* zeta(e) = sum_mn mu_mn Gamma_mn(e) / (1-e^2)^2 / vol (FP64 on the device),
+ * Gamma of TB/snippets.h:343-349; zeta_out: n_eps complex128. */
+int tbk_kubo_bastin_zeta(int32_t M, const double* mu, int32_t n_eps, const double* eps, double vol,
+                         double* zeta_out, void* stream);
+/* sigma(e) = -sum_mn Re(mu_mn) a_m a_n T_m(e) T_n(e) / (1-e^2) / R, the
+ * Kubo-Greenwood spectrum of TB/snippets.h:245-260 (FP64 on the device). */
+int tbk_kubo_greenwood_sigma(int32_t M, const double* mu, int32_t n_eps, const double* eps, double R,
+                             double* sigma_out, void* stream);
+/* Cumulative integration of zeta over the N Chebyshev nodes (descending, as the
+ * DCT produces them) from E = 0 outward, TB/snippets.h:421-449; writes
+ * n_out = N - 2*(N/24) ascending energies with Re / Im integrals. */
+int tbk_kubo_bastin_integrate(int32_t N, const double* eps, const double* zeta, double* E_out,
+                              double* re_out, double* im_out, int32_t* n_out);
+
+/* =========================================================================
  * Chebyshev moments without device allocation.  No counterpart in the
  * reference: it serves callers that may not allocate GPU memory while they run
  * (a fixed, fully reserved HBM budget; a host that lends device buffers but

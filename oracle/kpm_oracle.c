@@ -669,3 +669,31 @@ void tbo_greenwood_sigma(int32_t M, const double* mu, int32_t n_eps, const doubl
     sigma[e] = -sr / (1.0 - x * x) / R;
   }
 }
+
+/* Bastin integration, TB/snippets.h:421-449: drop N/24 nodes at each end,
+ * reverse to ascending energy, cumulative trapezoid from the first node above 0
+ * with the half-cell weights there.  zeta: N complex (interleaved). Returns n. */
+int32_t tbo_bastin_integrate(int32_t N, const double* eps, const double* zeta, double* E, double* re, double* im) {
+  int32_t cut = N / 24, n = N - 2 * cut;
+  double* zr = (double*)malloc(sizeof(double) * (size_t)n);
+  double* zi = (double*)malloc(sizeof(double) * (size_t)n);
+  for (int32_t k = 0; k < n; ++k) {
+    int32_t s = cut + (n - 1 - k);
+    E[k] = eps[s]; zr[k] = zeta[2 * s]; zi[k] = zeta[2 * s + 1];
+    re[k] = 0.0; im[k] = 0.0;
+  }
+  int32_t e0 = 0;
+  while (e0 < n && !(E[e0] > 0.0)) ++e0;       /* upper_bound(E, 0.0) */
+  re[e0] = (zr[e0] * 3 / 4 + zr[e0 - 1] / 4) * (E[e0] - E[e0 - 1]) / 2;
+  re[e0 - 1] = -(zr[e0] / 4 + zr[e0 - 1] * 3 / 4) * (E[e0] - E[e0 - 1]) / 2;
+  for (int32_t i = e0 + 1; i < n; ++i) {
+    re[i] = re[i - 1] + (zr[i] + zr[i - 1]) / 2 * (E[i] - E[i - 1]);
+    im[i] = im[i - 1] + (zi[i] + zi[i - 1]) / 2 * (E[i] - E[i - 1]);
+  }
+  for (int32_t i = e0 - 2; i >= 0; --i) {
+    re[i] = re[i + 1] - (zr[i] + zr[i + 1]) / 2 * (E[i + 1] - E[i]);
+    im[i] = im[i + 1] - (zi[i] + zi[i + 1]) / 2 * (E[i + 1] - E[i]);
+  }
+  free(zr); free(zi);
+  return n;
+}

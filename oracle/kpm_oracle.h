@@ -158,6 +158,9 @@ void tbo_bastin_zeta(int32_t M, const double* mu, int32_t n_eps, const double* e
 void tbo_greenwood_sigma(int32_t M, const double* mu, int32_t n_eps, const double* eps,
                          double R, double* sigma_out);
 
+/* Bastin cumulative integration (TB/snippets.h:421-449); returns the count. */
+int32_t tbo_bastin_integrate(int32_t N, const double* eps, const double* zeta, double* E, double* re, double* im);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,7 @@ def lib():
             "tbo_mu_nm": (None, [i32, i64, vp, vp, vp]),
             "tbo_bastin_zeta": (None, [i32, vp, i32, vp, d, vp]),
             "tbo_greenwood_sigma": (None, [i32, vp, i32, vp, d, vp]),
+            "tbo_bastin_integrate": (i32, [i32, vp, vp, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -247,3 +248,44 @@ def greenwood_sigma(mu, eps, R):
     out = np.zeros(len(eps))
     lib().tbo_greenwood_sigma(mu.shape[0], _p(mu), len(eps), _p(eps), float(R), _p(out))
     return out
+
+
+def bastin_integrate(eps, zeta):
+    eps = np.ascontiguousarray(eps, dtype=np.float64)
+    zeta = np.ascontiguousarray(zeta, dtype=np.complex128)
+    N = len(eps)
+    E, re, im = np.zeros(N), np.zeros(N), np.zeros(N)
+    n = lib().tbo_bastin_integrate(N, _p(eps), _p(zeta), _p(E), _p(re), _p(im))
+    return E[:n], re[:n], im[:n]
+
+
+def kubo_mu(n, cp, ri, v, M, kets, AL=None, BL=None, AR=None, BR=None, g=None):
+    """mu_mn = sum conj(g_m AL T_m BL r) (g_n AR T_n BR r) in FP64; operators are
+    (cp, ri, v) CSC triples or None."""
+    def app(op, X):
+        if op is None:
+            return X
+        ocp, ori, ov = op
+        Y = np.zeros_like(X)
+        lib().tbo_csc_mult(n, _p(ocp), _p(ori), _p(np.ascontiguousarray(ov)), int(np.iscomplexobj(ov)), X.shape[1],
+                           _p(np.asfortranarray(X)), _p(Y))
+        return Y
+
+    kets = np.asfortranarray(kets, dtype=np.complex128)
+    R = kets.shape[1]
+
+    def side(A, B):
+        x0 = np.asfortranarray(app(B, kets))
+        blocks = cheb_blocks(n, cp, ri, v, M, x0)               # (M, R, n)
+        out = np.zeros((M, R * n), dtype=np.complex128)
+        for m in range(M):
+            blk = np.asfortranarray(blocks[m].T)                  # n x R
+            out[m] = np.asfortranarray(app(A, blk)).T.reshape(-1)
+        return out
+
+    Lb = side(AL, BL)
+    Rb = side(AR, BR)
+    mu = mu_nm(Lb, Rb)
+    if g is not None:
+        mu = mu * np.outer(g, g)
+    return mu

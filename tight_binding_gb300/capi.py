@@ -33,6 +33,8 @@ BUILD_SPARSE = 0
 BUILD_PERIODIC_BARE = 1
 BUILD_BARE = 2
 
+MU_CUDA_CORE, MU_TENSOR = 0, 1
+
 KERNEL_DIRICHLET, KERNEL_FEJER, KERNEL_LORENTZ, KERNEL_JACKSON, KERNEL_LANCZOS, KERNEL_WANG_ZUNGER = range(6)
 
 _i32, _i64, _u64, _d, _vp, _cp = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_void_p, C.c_char_p
@@ -83,6 +85,10 @@ SIGNATURES = {
     "tbk_green_imag_eval": (C.c_int, [_i32, _vp, _vp, _i32, _vp, _vp, _vp]),
     "tbk_green_imag_fft": (C.c_int, [_i32, _vp, _vp, _i32, _vp, _vp, _vp]),
     "tbk_dos_from_moments": (C.c_int, [_i32, _vp, _i32, _d, _d, _d, _i32, _vp, _vp, _vp]),
+    "tbk_kubo_mu": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i32, _i32, _u64, _vp, _i32, _d, _d, _i32, _d, _vp, _vp]),
+    "tbk_kubo_bastin_zeta": (C.c_int, [_i32, _vp, _i32, _vp, _d, _vp, _vp]),
+    "tbk_kubo_greenwood_sigma": (C.c_int, [_i32, _vp, _i32, _vp, _d, _vp, _vp]),
+    "tbk_kubo_bastin_integrate": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _pi32]),
     "tbk_cheb_moments_noalloc": (C.c_int, [_i32, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp]),
 }
 

@@ -149,8 +149,8 @@ template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET>
 __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     int32_t n, int32_t n_tiles, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
     const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
-    typename C2<F>::T* y, const typename C2<F>::T* __restrict__ bras, double* __restrict__ part,
-    int store, int reverse, int gather, int pf_dist) {
+    typename C2<F>::T* y, const typename C2<F>::T* pv, const typename C2<F>::T* __restrict__ bras,
+    double* __restrict__ part, int store, int reverse, int gather, int pf_dist) {
   using CT = typename C2<F>::T;
   constexpr int VPL = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
   constexpr int LPR = R / VPL;             // lanes per row
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
           const uint32_t vb = (uint32_t)nr * (uint32_t)(R * sizeof(CT));
           if ((vb & 15u) == 0) {
             bulk_prefetch_l2(x + rf * R, vb);
-            if (!FIRST) bulk_prefetch_l2(y + rf * R, vb);
+            if (!FIRST) bulk_prefetch_l2(pv + rf * R, vb);
             if (BRAKET) bulk_prefetch_l2(bras + rf * R, vb);
           }
         }
@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     const int64_t me = (int64_t)r * LPR + sub;
     const LaneV<F, VPL> xs = ld_ro<F, VPL>(x + me * VPL);
     LaneV<F, VPL> prev;
-    if constexpr (!FIRST) prev = ld_stream<F, VPL>(y + me * VPL);
+    if constexpr (!FIRST) prev = ld_stream<F, VPL>(pv + me * VPL);   // pv == y: in place
     LaneV<F, VPL> acc;
 #pragma unroll
     for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
@@ -360,6 +360,7 @@ struct StepArgs {
   const void* diag;
   const void* x;
   void* y;
+  const void* pv;      // v_{n-1}; equal to y for the in-place recursion
   const void* bras;
   double* part;
   int store, reverse, gather, pf_dist;
@@ -370,12 +371,13 @@ static int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
   using CT = typename C2<F>::T;
   auto x = static_cast<const CT*>(a.x);
   auto y = static_cast<CT*>(a.y);
+  auto pv = static_cast<const CT*>(a.pv ? a.pv : a.y);
   auto b = static_cast<const CT*>(a.bras);
   auto ev = static_cast<const F*>(a.eval);
   auto dg = static_cast<const F*>(a.diag);
 #define TBK_STEP(FI, BR)                                                                   \
   kpm_step_kernel<F, R, CPLX_H, FI, BR><<<grid, kStepThreads, 0, st>>>(                    \
-      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, b, a.part, a.store, a.reverse, a.gather, a.pf_dist)
+      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist)
   if (first) { if (braket) TBK_STEP(true, true); else TBK_STEP(true, false); }
   else { if (braket) TBK_STEP(false, true); else TBK_STEP(false, false); }
 #undef TBK_STEP
@@ -473,6 +475,74 @@ static int rows_per_tile(int prec, int Rc) {
   return (32 / lpr) * kStepWarps;
 }
 
+// ---------------------------------------------------------------- internal API
+// (used by the Kubo block recursions in kubo.cu)
+int step_config(tbk_sparse_s* A, int Rc, bool fp64, int* grid, int* n_tiles, cudaStream_t st) {
+  TBK_TRY(ensure_ell(A, st));
+  const int rpt = rows_per_tile(fp64 ? TBK_PREC_FP64 : TBK_PREC_MIXED, Rc);
+  *n_tiles = (A->rows + rpt - 1) / rpt;
+  int occ = 1;
+  const bool cplx = A->is_complex != 0;
+#define OCC2(F)                                                                                          \
+  switch (Rc) {                                                                                          \
+    case 1: occ = cplx ? occupancy_blocks<F, true, 1>() : occupancy_blocks<F, false, 1>(); break;        \
+    case 2: occ = cplx ? occupancy_blocks<F, true, 2>() : occupancy_blocks<F, false, 2>(); break;        \
+    case 4: occ = cplx ? occupancy_blocks<F, true, 4>() : occupancy_blocks<F, false, 4>(); break;        \
+    case 8: occ = cplx ? occupancy_blocks<F, true, 8>() : occupancy_blocks<F, false, 8>(); break;        \
+    case 16: occ = cplx ? occupancy_blocks<F, true, 16>() : occupancy_blocks<F, false, 16>(); break;     \
+    default: occ = cplx ? occupancy_blocks<F, true, 32>() : occupancy_blocks<F, false, 32>(); break;     \
+  }
+  if (fp64) { OCC2(double) } else { OCC2(float) }
+#undef OCC2
+  *grid = std::max(1, std::min(*n_tiles, sm_count() * occ));
+  return TBK_OK;
+}
+
+int step_any(tbk_sparse_s* A, int Rc, bool fp64, const void* x, void* y, const void* pv, bool first, double* part,
+             int grid, int n_tiles, cudaStream_t st) {
+  StepArgs a;
+  a.n = A->rows;
+  a.n_tiles = n_tiles;
+  a.n_slices = A->ell.n_slices;
+  a.err = nullptr;
+  a.soff = A->ell.slice_off.as<int32_t>();
+  a.ecol = A->ell.col.as<int32_t>();
+  a.eval = fp64 ? A->ell.val64.p : A->ell.val32.p;
+  a.diag = fp64 ? A->ell.diag64.p : A->ell.diag32.p;
+  a.x = x;
+  a.y = y;
+  a.pv = first ? y : pv;
+  a.bras = nullptr;
+  a.part = part;
+  a.store = 1;
+  a.reverse = 0;
+  a.gather = 1;
+  a.pf_dist = 1;
+  if (fp64)
+    return A->is_complex ? launch_step<double, true>(Rc, a, first, false, grid, st)
+                         : launch_step<double, false>(Rc, a, first, false, grid, st);
+  return A->is_complex ? launch_step<float, true>(Rc, a, first, false, grid, st)
+                       : launch_step<float, false>(Rc, a, first, false, grid, st);
+}
+
+int load_block_any(bool fp64, int32_t n, int32_t R, int32_t r0, int32_t Rp, const double2* src, void* dst,
+                   cudaStream_t st) {
+  dim3 g((unsigned)((n + 31) / 32), (unsigned)((Rp + 31) / 32)), b(32, 8);
+  if (fp64) load_block_kernel<double><<<g, b, 0, st>>>(n, R, r0, std::min(Rp, R - r0), Rp, src, static_cast<double2*>(dst));
+  else load_block_kernel<float><<<g, b, 0, st>>>(n, R, r0, std::min(Rp, R - r0), Rp, src, static_cast<float2*>(dst));
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
+}
+
+int random_block_any(bool fp64, int32_t n, int32_t R, int32_t r0, int32_t Rp, uint64_t seed, void* dst,
+                     cudaStream_t st) {
+  int64_t tot = (int64_t)n * Rp;
+  if (fp64) random_block_kernel<double><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(n, R, r0, Rp, seed, static_cast<double2*>(dst));
+  else random_block_kernel<float><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(n, R, r0, Rp, seed, static_cast<float2*>(dst));
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
+}
+
 }  // namespace tbk
 
 using namespace tbk;
@@ -553,6 +623,7 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
       a.diag = mixed ? E.diag32.p : E.diag64.p;
       a.x = x;
       a.y = y;
+      a.pv = y;
       a.bras = braket ? P->bras.p : nullptr;
       a.part = P->part.as<double>() + (((int64_t)ch * n_steps + s) * 2) * G;
       const bool last_dot = doubling && s == n_steps - 1 && s > 0;   // dots only, no product

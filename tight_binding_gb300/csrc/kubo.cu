@@ -1,0 +1,382 @@
+// kubo.cu — Kubo conductivities from double-Chebyshev moments.
+//
+//   aL_m = g_m AL T_m(H~) BL |r>,   aR_n = g_n AR T_n(H~) BR |r>
+//   mu_mn = sum_{sites, r} conj(aL_m) aR_n                        (a GEMM L^H R)
+// Bastin sigma_xy: AL = BL = 1, AR = v_x, BR = v_y        (TB/snippets.h:306-456)
+// Greenwood sigma_xx: AL = BL = v_x, AR = BR = 1           (TB/snippets.h:225-304)
+// generate_V_moments: as Greenwood with the Dirichlet kernel (TB/snippets.h:491-518)
+//
+// The stored blocks (Cheb_first_kind_seq_on_bases, TB/numerical.h:333-344) are
+// complex64 site-major blocks in HBM.  They are produced by the fused recursion
+// step of kpm.cu running in complex128 on a three-block ring (the outer operator
+// AL/AR applied after each step), each stored value rounded to complex64 once.
+// Random vectors are processed in chunks so that both sides fit the block
+// budget; mu accumulates over chunks in FP64 on the device.  The Gamma
+// contractions (FP64) and the Bastin integration follow TB/snippets.h:343-449.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <vector>
+
+#include "tbk_internal.h"
+
+namespace tbk {
+
+int mu_gemm_tc(const float2* L, const float2* Rb, int32_t M, int64_t K, int64_t ldb, double* mu_acc,
+               cudaStream_t st);   // gemm_tc.cu (tensor cores, split TF32)
+
+namespace {
+
+// ------------------------------------------------------------------ CUDA-core GEMM
+// C[m][n] += sum_k conj(L[m][k]) R[n][k] for a K range per CTA (split-K);
+// FP32 products, FP32 sums over 32 terms promoted to FP64, FP64 partial tiles.
+constexpr int kGT = 32;      // output tile (complex) per CTA side
+constexpr int kGK = 32;      // K chunk staged in shared memory
+
+__global__ void __launch_bounds__(256) mu_gemm_cc_kernel(const float2* __restrict__ L, const float2* __restrict__ Rb,
+                                                         int32_t M, int64_t K, int64_t ld, int64_t ksplit,
+                                                         double2* __restrict__ part) {
+  __shared__ float2 Ls[kGT][kGK + 1], Rs[kGT][kGK + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int32_t m0 = blockIdx.y * kGT, n0 = blockIdx.x * kGT;
+  const int64_t k0 = (int64_t)blockIdx.z * ksplit;
+  const int64_t k1 = min(K, k0 + ksplit);
+  float ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
+  double dr[2][2] = {{0, 0}, {0, 0}}, di[2][2] = {{0, 0}, {0, 0}};
+  for (int64_t kb = k0; kb < k1; kb += kGK) {
+    for (int q = threadIdx.x; q < kGT * kGK; q += 256) {
+      const int row = q / kGK, kk = q % kGK;
+      const int64_t k = kb + kk;
+      float2 z = make_float2(0.f, 0.f);
+      Ls[row][kk] = (m0 + row < M && k < k1) ? L[(int64_t)(m0 + row) * ld + k] : z;
+      Rs[row][kk] = (n0 + row < M && k < k1) ? Rb[(int64_t)(n0 + row) * ld + k] : z;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < kGK; ++kk) {
+      const float2 a0 = Ls[ty * 2][kk], a1 = Ls[ty * 2 + 1][kk];
+      const float2 b0 = Rs[tx * 2][kk], b1 = Rs[tx * 2 + 1][kk];
+      const float2 a[2] = {a0, a1}, b[2] = {b0, b1};
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          // conj(a) * b
+          ar[i][j] += a[i].x * b[j].x + a[i].y * b[j].y;
+          ai[i][j] += a[i].x * b[j].y - a[i].y * b[j].x;
+        }
+    }
+    __syncthreads();
+    // FP32 sums cover one 32-term chunk only: long FP32 accumulations lose
+    // accuracy where the sum is much smaller than its terms (mu_nm at large m, n)
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) { dr[i][j] += ar[i][j]; di[i][j] += ai[i][j]; ar[i][j] = 0; ai[i][j] = 0; }
+  }
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) {
+      dr[i][j] += ar[i][j];
+      di[i][j] += ai[i][j];
+      const int32_t m = m0 + ty * 2 + i, n = n0 + tx * 2 + j;
+      if (m < M && n < M) part[((int64_t)blockIdx.z * M + m) * M + n] = make_double2(dr[i][j], di[i][j]);
+    }
+}
+
+__global__ void mu_split_reduce_kernel(const double2* __restrict__ part, int32_t M, int32_t nsplit,
+                                       double2* __restrict__ acc) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (int64_t)M * M) return;
+  double r = 0.0, i = 0.0;
+  for (int32_t s = 0; s < nsplit; ++s) { const double2 v = part[(int64_t)s * M * M + q]; r += v.x; i += v.y; }
+  acc[q].x += r;
+  acc[q].y += i;
+}
+
+// complex128 work block -> complex64 stored block (one rounding per element)
+__global__ void round_block_kernel(const double2* __restrict__ src, float2* __restrict__ dst, int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    dst[q] = make_float2(__double2float_rn(src[q].x), __double2float_rn(src[q].y));
+}
+
+__global__ void mu_kernel_scale_kernel(double2* __restrict__ mu, const double* __restrict__ g, int32_t M) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (int64_t)M * M) return;
+  const double s = g[q / M] * g[q % M];
+  mu[q].x *= s;
+  mu[q].y *= s;
+}
+
+// ------------------------------------------------------------------ Gamma contractions (FP64)
+// zeta(e) = sum_mn mu_mn a_m a_n [(e - i n s) e^{i n th} T_m + (e + i m s) e^{-i m th} T_n] / (1-e^2)^2 / vol
+//         = sum_m a_m T_m (sum_n mu_mn P_n) + sum_m P'_m (sum_n mu_mn a_n T_n),
+//   P_n = a_n (e - i n s) e^{i n th},   P'_m = a_m (e + i m s) e^{-i m th}.
+__global__ void bastin_zeta_kernel(const double2* __restrict__ mu, int32_t M, const double* __restrict__ eps,
+                                   double vol, double2* __restrict__ zeta) {
+  extern __shared__ double2 sm[];
+  double2* P = sm;          // P_n
+  double2* Q = sm + M;      // a_n T_n (real, stored as complex)
+  const double e = eps[blockIdx.x];
+  const double s = sqrt(1.0 - e * e), th = acos(e);
+  for (int n = threadIdx.x; n < M; n += blockDim.x) {
+    double sn, cn;
+    sincos(n * th, &sn, &cn);
+    const double an = n == 0 ? 1.0 : 2.0;
+    // (e - i n s)(cn + i sn)
+    P[n] = make_double2(an * (e * cn + n * s * sn), an * (e * sn - n * s * cn));
+    Q[n] = make_double2(an * cn, 0.0);
+  }
+  __syncthreads();
+  double zr = 0.0, zi = 0.0;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    double sm_, cm;
+    sincos(m * th, &sm_, &cm);
+    const double am = m == 0 ? 1.0 : 2.0;
+    double r1 = 0.0, i1 = 0.0, r2 = 0.0, i2 = 0.0;
+    const double2* row = mu + (int64_t)m * M;
+    for (int n = 0; n < M; ++n) {
+      const double2 u = row[n];
+      r1 += u.x * P[n].x - u.y * P[n].y;
+      i1 += u.x * P[n].y + u.y * P[n].x;
+      r2 += u.x * Q[n].x;
+      i2 += u.y * Q[n].x;
+    }
+    const double qm = am * cm;                                    // a_m T_m
+    const double pr = am * (e * cm + m * s * sm_), pi = am * (-e * sm_ + m * s * cm);   // (e + i m s)(cm - i sm)
+    zr += qm * r1 + (pr * r2 - pi * i2);
+    zi += qm * i1 + (pr * i2 + pi * r2);
+  }
+  __shared__ double red[2][32];
+  for (int o = 16; o > 0; o >>= 1) { zr += __shfl_xor_sync(0xffffffffu, zr, o); zi += __shfl_xor_sync(0xffffffffu, zi, o); }
+  if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = zr; red[1][threadIdx.x >> 5] = zi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { a += red[0][w]; b += red[1][w]; }
+    const double den = (1.0 - e * e) * (1.0 - e * e) * vol;
+    zeta[blockIdx.x] = make_double2(a / den, b / den);
+  }
+}
+
+// sigma(e) = -sum_mn Re(mu_mn) a_m a_n T_m(e) T_n(e) / (1 - e^2) / R
+__global__ void greenwood_kernel(const double2* __restrict__ mu, int32_t M, const double* __restrict__ eps, double R,
+                                 double* __restrict__ sigma) {
+  extern __shared__ double2 sm[];
+  double* T = reinterpret_cast<double*>(sm);
+  const double e = eps[blockIdx.x];
+  const double th = acos(e);
+  for (int n = threadIdx.x; n < M; n += blockDim.x) T[n] = (n == 0 ? 1.0 : 2.0) * cos(n * th);
+  __syncthreads();
+  double acc = 0.0;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    double r = 0.0;
+    const double2* row = mu + (int64_t)m * M;
+    for (int n = 0; n < M; ++n) r += row[n].x * T[n];
+    acc += T[m] * r;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += red[w];
+    sigma[blockIdx.x] = -a / (1.0 - e * e) / R;
+  }
+}
+
+int pick_chunk(int R) {
+  int c = 1;
+  while (c < R && c < 32) c <<= 1;
+  return c;
+}
+
+}  // namespace
+}  // namespace tbk
+
+using namespace tbk;
+
+extern "C" {
+
+int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_sparse BR, int32_t M, int32_t R,
+                uint64_t seed, const double* kets, int32_t kernel_kind, double kp0, double kp1, int32_t flags,
+                double block_budget_gb, double* mu_out, void* stream) {
+  if (!Ht || !mu_out) return fail(TBK_ERR_INVALID, "tbk_kubo_mu: null argument");
+  if (M < 1 || R < 1) return fail(TBK_ERR_INVALID, "tbk_kubo_mu: M and R must be >= 1");
+  if (Ht->rows != Ht->cols) return fail(TBK_ERR_INVALID, "tbk_kubo_mu: H must be square");
+  tbk_sparse ops[4] = {AL, BL, AR, BR};
+  for (auto* o : ops)
+    if (o && (o->rows != Ht->rows || o->cols != Ht->cols)) return fail(TBK_ERR_INVALID, "tbk_kubo_mu: operator size mismatch");
+  cudaStream_t st = as_stream(stream);
+  const int32_t n = Ht->rows;
+  TBK_TRY(ensure_ell(Ht, st));
+  for (auto* o : ops) if (o) TBK_TRY(ensure_ell(o, st));
+  const int64_t n_pad = (int64_t)Ht->ell.n_slices * 32;
+  // chunk of random vectors: both stored sides within the budget
+  int Rc = pick_chunk(R);
+  const double budget = (block_budget_gb > 0 ? block_budget_gb : 40.0) * 1e9;
+  while (Rc > 1 && 2.0 * M * n_pad * Rc * 8.0 > budget) Rc >>= 1;
+  if (2.0 * M * n_pad * Rc * 8.0 > budget)
+    return fail(TBK_ERR_BUDGET, "stored Chebyshev blocks need %.1f GB > budget %.1f GB", 2.0 * M * n_pad * 8.0 / 1e9,
+                budget / 1e9);
+  const int64_t blk = n_pad * Rc;                       // complex entries per block
+  // stored blocks: complex64; recursion and operator applications: complex128
+  // work blocks (the Chebyshev recursion accumulates rounding error near the band
+  // edges, where the Kubo weights 1/(1-e^2)^2 are largest; each stored value is
+  // rounded to complex64 exactly once)
+  DevBuf Ls, Rs, work, partd, part, macc, gdev, kstage;
+  TBK_TRY(Ls.alloc(sizeof(float2) * blk * M));
+  TBK_TRY(Rs.alloc(sizeof(float2) * blk * M));
+  TBK_TRY(work.alloc(sizeof(double2) * blk * 6));
+  TBK_CUDA(cudaMemsetAsync(Ls.p, 0, Ls.bytes, st));
+  TBK_CUDA(cudaMemsetAsync(Rs.p, 0, Rs.bytes, st));
+  TBK_CUDA(cudaMemsetAsync(work.p, 0, work.bytes, st));
+  TBK_TRY(macc.alloc(sizeof(double2) * (size_t)M * M));
+  TBK_CUDA(cudaMemsetAsync(macc.p, 0, macc.bytes, st));
+  if (kets) {
+    TBK_TRY(kstage.alloc(sizeof(double2) * (size_t)n * R));
+    TBK_CUDA(cudaMemcpyAsync(kstage.p, kets, sizeof(double2) * (size_t)n * R, cudaMemcpyHostToDevice, st));
+  }
+  int grid = 1, n_tiles = 1;
+  TBK_TRY(step_config(Ht, Rc, true, &grid, &n_tiles, st));
+  int gmax = grid;
+  for (auto* o : ops)
+    if (o) { int g2, t2; TBK_TRY(step_config(o, Rc, true, &g2, &t2, st)); gmax = std::max(gmax, g2); }
+  TBK_TRY(partd.alloc(sizeof(double) * 2 * gmax));
+  double2* wb = work.as<double2>();
+  double2* v0 = wb + 5 * blk;
+  auto apply = [&](tbk_sparse_s* A, const double2* x, double2* y) -> int {   // y = A x (FP64)
+    int g, t;
+    TBK_TRY(step_config(A, Rc, true, &g, &t, st));
+    return step_any(A, Rc, true, x, y, nullptr, true, partd.as<double>(), g, t, st);
+  };
+  auto round_to = [&](const double2* src, float2* dst) -> int {
+    round_block_kernel<<<(unsigned)std::min<int64_t>((blk + 255) / 256, 65535), 256, 0, st>>>(src, dst, blk);
+    TBK_CHECK_LAUNCH();
+    return TBK_OK;
+  };
+  // one side: store[m] = Aout T_m(H~) (Bin v0), m < M
+  auto side = [&](tbk_sparse_s* Aout, tbk_sparse_s* Bin, float2* store) -> int {
+    double2* r[3] = {wb, wb + blk, wb + 2 * blk};
+    double2* tmpA = wb + 3 * blk;
+    if (Bin) TBK_TRY(apply(Bin, v0, r[0]));
+    else TBK_CUDA(cudaMemcpyAsync(r[0], v0, sizeof(double2) * blk, cudaMemcpyDeviceToDevice, st));
+    for (int32_t m = 0; m < M; ++m) {
+      double2* y = r[m % 3];
+      if (m >= 1) {
+        const double2* x = r[(m - 1) % 3];
+        const double2* pv = m >= 2 ? r[(m - 2) % 3] : nullptr;
+        TBK_TRY(step_any(Ht, Rc, true, x, y, pv, m == 1, partd.as<double>(), grid, n_tiles, st));
+      }
+      if (Aout) { TBK_TRY(apply(Aout, y, tmpA)); TBK_TRY(round_to(tmpA, store + (int64_t)m * blk)); }
+      else TBK_TRY(round_to(y, store + (int64_t)m * blk));
+    }
+    return TBK_OK;
+  };
+  const bool use_tc = (flags & 1) != 0;
+  const int64_t ksplit = 16384;
+  const int32_t nsplit = (int32_t)((blk + ksplit - 1) / ksplit);
+  if (!use_tc) TBK_TRY(part.alloc(sizeof(double2) * (size_t)nsplit * M * M));
+  for (int32_t r0 = 0; r0 < R; r0 += Rc) {
+    if (kets) TBK_TRY(load_block_any(true, n, R, r0, Rc, kstage.as<double2>(), v0, st));
+    else TBK_TRY(random_block_any(true, n, R, r0, Rc, seed, v0, st));
+    TBK_TRY(side(AL, BL, Ls.as<float2>()));
+    TBK_TRY(side(AR, BR, Rs.as<float2>()));
+    if (use_tc) {
+      TBK_TRY(mu_gemm_tc(Ls.as<float2>(), Rs.as<float2>(), M, blk, blk, macc.as<double>(), st));
+    } else {
+      dim3 g((M + kGT - 1) / kGT, (M + kGT - 1) / kGT, nsplit);
+      mu_gemm_cc_kernel<<<g, 256, 0, st>>>(Ls.as<float2>(), Rs.as<float2>(), M, blk, blk, ksplit, part.as<double2>());
+      TBK_CHECK_LAUNCH();
+      mu_split_reduce_kernel<<<(unsigned)(((int64_t)M * M + 255) / 256), 256, 0, st>>>(part.as<double2>(), M, nsplit,
+                                                                                       macc.as<double2>());
+      TBK_CHECK_LAUNCH();
+    }
+  }
+  // kernel factors g_m g_n (FP64)
+  std::vector<double> g(M);
+  TBK_TRY(tbk_kernel_seq(kernel_kind, M, kp0, kp1, g.data()));
+  TBK_TRY(gdev.alloc(sizeof(double) * M));
+  TBK_CUDA(cudaMemcpyAsync(gdev.p, g.data(), sizeof(double) * M, cudaMemcpyHostToDevice, st));
+  mu_kernel_scale_kernel<<<(unsigned)(((int64_t)M * M + 255) / 256), 256, 0, st>>>(macc.as<double2>(), gdev.as<double>(), M);
+  TBK_CHECK_LAUNCH();
+  TBK_CUDA(cudaMemcpyAsync(mu_out, macc.p, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  return TBK_OK;
+}
+
+int tbk_kubo_bastin_zeta(int32_t M, const double* mu, int32_t n_eps, const double* eps, double vol, double* zeta_out,
+                         void* stream) {
+  if (M < 1 || !mu || n_eps < 0 || (n_eps && (!eps || !zeta_out))) return fail(TBK_ERR_INVALID, "tbk_kubo_bastin_zeta: bad argument");
+  if (n_eps == 0) return TBK_OK;
+  cudaStream_t st = as_stream(stream);
+  DevBuf dm, de, dz;
+  TBK_TRY(dm.alloc(sizeof(double2) * (size_t)M * M));
+  TBK_TRY(de.alloc(sizeof(double) * n_eps));
+  TBK_TRY(dz.alloc(sizeof(double2) * n_eps));
+  TBK_CUDA(cudaMemcpyAsync(dm.p, mu, sizeof(double2) * (size_t)M * M, cudaMemcpyHostToDevice, st));
+  TBK_CUDA(cudaMemcpyAsync(de.p, eps, sizeof(double) * n_eps, cudaMemcpyHostToDevice, st));
+  const size_t smem = sizeof(double2) * 2 * M;
+  if (smem > 48 * 1024) TBK_CUDA(cudaFuncSetAttribute(bastin_zeta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  bastin_zeta_kernel<<<n_eps, 256, smem, st>>>(dm.as<double2>(), M, de.as<double>(), vol, dz.as<double2>());
+  TBK_CHECK_LAUNCH();
+  TBK_CUDA(cudaMemcpyAsync(zeta_out, dz.p, sizeof(double2) * n_eps, cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  return TBK_OK;
+}
+
+int tbk_kubo_greenwood_sigma(int32_t M, const double* mu, int32_t n_eps, const double* eps, double R,
+                             double* sigma_out, void* stream) {
+  if (M < 1 || !mu || n_eps < 0 || (n_eps && (!eps || !sigma_out)) || !(R > 0))
+    return fail(TBK_ERR_INVALID, "tbk_kubo_greenwood_sigma: bad argument");
+  if (n_eps == 0) return TBK_OK;
+  cudaStream_t st = as_stream(stream);
+  DevBuf dm, de, ds;
+  TBK_TRY(dm.alloc(sizeof(double2) * (size_t)M * M));
+  TBK_TRY(de.alloc(sizeof(double) * n_eps));
+  TBK_TRY(ds.alloc(sizeof(double) * n_eps));
+  TBK_CUDA(cudaMemcpyAsync(dm.p, mu, sizeof(double2) * (size_t)M * M, cudaMemcpyHostToDevice, st));
+  TBK_CUDA(cudaMemcpyAsync(de.p, eps, sizeof(double) * n_eps, cudaMemcpyHostToDevice, st));
+  greenwood_kernel<<<n_eps, 256, sizeof(double2) * M, st>>>(dm.as<double2>(), M, de.as<double>(), R, ds.as<double>());
+  TBK_CHECK_LAUNCH();
+  TBK_CUDA(cudaMemcpyAsync(sigma_out, ds.p, sizeof(double) * n_eps, cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  return TBK_OK;
+}
+
+// Bastin: drop N/24 nodes at each end, ascending order, cumulative trapezoid from
+// E = 0 outward with the half-cell weights of TB/snippets.h:421-449 (host, O(N)).
+int tbk_kubo_bastin_integrate(int32_t N, const double* eps, const double* zeta, double* E_out, double* re_out,
+                              double* im_out, int32_t* n_out) {
+  if (N < 4 || !eps || !zeta || !E_out || !re_out || !im_out || !n_out)
+    return fail(TBK_ERR_INVALID, "tbk_kubo_bastin_integrate: bad argument");
+  const int32_t cut = N / 24;
+  const int32_t n = N - 2 * cut;
+  std::vector<double> E(n), zr(n), zi(n);
+  for (int32_t k = 0; k < n; ++k) {     // drop(cut) | take(N - 2 cut) | reverse
+    const int32_t src = cut + (n - 1 - k);
+    E[k] = eps[src];
+    zr[k] = zeta[2 * src];
+    zi[k] = zeta[2 * src + 1];
+  }
+  const int32_t e0 = (int32_t)(std::upper_bound(E.begin(), E.end(), 0.0) - E.begin());
+  if (e0 < 1 || e0 >= n) return fail(TBK_ERR_INVALID, "bastin integration: E = 0 not inside the node range");
+  std::vector<double> ri(n, 0.0), ii(n, 0.0);
+  ri[e0] = (zr[e0] * 3 / 4 + zr[e0 - 1] / 4) * (E[e0] - E[e0 - 1]) / 2;
+  ri[e0 - 1] = -(zr[e0] / 4 + zr[e0 - 1] * 3 / 4) * (E[e0] - E[e0 - 1]) / 2;
+  for (int32_t i = e0 + 1; i < n; ++i) {
+    ri[i] = ri[i - 1] + (zr[i] + zr[i - 1]) / 2 * (E[i] - E[i - 1]);
+    ii[i] = ii[i - 1] + (zi[i] + zi[i - 1]) / 2 * (E[i] - E[i - 1]);
+  }
+  for (int32_t i = e0 - 2; i >= 0; --i) {
+    ri[i] = ri[i + 1] - (zr[i] + zr[i + 1]) / 2 * (E[i + 1] - E[i]);
+    ii[i] = ii[i + 1] - (zi[i] + zi[i + 1]) / 2 * (E[i + 1] - E[i]);
+  }
+  for (int32_t k = 0; k < n; ++k) { E_out[k] = E[k]; re_out[k] = ri[k]; im_out[k] = ii[k]; }
+  *n_out = n;
+  return TBK_OK;
+}
+
+}  // extern "C"
