@@ -353,6 +353,57 @@ def run_gpu(args):
     return 0
 
 
+def peaks_tensor():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        # TF32 dense rate is half the BF16 rate on this part; reported against half the measured cuBLAS BF16 burst
+        return float(d["bf16_tflops"]) / 2.0, "half of measured bf16 burst (TF32 = BF16/2)"
+    return 1900.0 / 2.0, "half of fallback bf16"
+
+
+def run_kubo(config: int, tensor: bool = True):
+    """Kubo legs: config 3 (Bastin sigma_xy, square 256^2 open-x / periodic-y, Landau
+    flux 1/64, M = 512, R = 16, seed 2) or config 5 (Greenwood sigma_xx, FCC 128^3
+    periodic, on-site U[-1,1] seed 4, M = 1024, R = 8)."""
+    import tight_binding_gb300 as tb
+
+    t0 = time.perf_counter()
+    if config == 3:
+        L, M, R = 256, 512, 16
+        X = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (L, L))
+        G = np.zeros((3, 3))
+        G[1, 0] = 2 * np.pi / 64
+        X.set_gauge_linear(G, np.zeros(3))
+        H = X.get_Hamiltonian_periodic_extend_bare_sparse([0, 1], complex)
+        out = tb.conductivity_Kubo_Bastin(H, X.op_position(0), X.op_position(1), M, -4.0, 4.0, R=R, seed=2,
+                                          tensor=tensor)
+        result = {"E_F_points": int(len(out["E"])), "sigma_xy_at_E0": float(out["sigma_re"][len(out["E"]) // 2])}
+        workload = "Kubo-Bastin sigma_xy: square 256x256 open-x/periodic-y, Landau flux 1/64, M=512, R=16 seed 2"
+    else:
+        L, M, R = 128, 1024, 8
+        X = tb.PartialLattice(tb.FCC().add_hopping("A", 1, 1.0), (L, L, L))
+        X.set_scalar_disorder(2.0, 4)
+        H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1, 1], complex)
+        eps, sigma, mu = tb.conductivity_spectrum(H, X.op_position(0), X.op_position(1), M, R=R, seed=4,
+                                                  E_min=-13.0, E_max=13.0, tensor=tensor)
+        result = {"energies": int(len(eps)), "sigma_xx_max": float(np.max(sigma))}
+        workload = "Kubo-Greenwood sigma_xx: FCC 128^3 periodic, disorder U[-1,1] seed 4, M=1024, R=8"
+    wall = time.perf_counter() - t0
+    tmg = tb.kubo_last_timing()
+    peak, src = peaks_tensor()
+    useful = tmg["gemm_flops"] / (3.0 if tensor else 1.0)       # one complex GEMM = 8 M^2 K real flops
+    line = {"workload": workload, "path": "tcgen05 3xTF32" if tensor else "CUDA-core FP32",
+            "wall_s": wall, "blocks_ms": tmg["ms_blocks"], "gemm_ms": tmg["ms_gemm"], "chunks": tmg["chunks"],
+            "gemm_tflops_issued": tmg["gemm_flops"] / (tmg["ms_gemm"] / 1e3) / 1e12,
+            "gemm_tflops_useful": useful / (tmg["ms_gemm"] / 1e3) / 1e12,
+            "tensor_peak_tflops": peak, "tensor_peak_source": src,
+            "blocks_GBps": tmg["block_bytes"] / (tmg["ms_blocks"] / 1e3) / 1e9, **result}
+    if tensor:
+        line["tensor_util"] = line["gemm_tflops_issued"] / peak
+    return line
+
+
 def run_kernel_only(args):
     """Small case of the same kernel for ncu captures: one mixed-precision DoS
     solve (doubling) on a honeycomb of --cells^2 cells, R = 32."""
@@ -390,11 +441,17 @@ def main():
     ap.add_argument("--moments", type=int, default=32)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--staged", action="store_true", help="TMA-staged warp-specialised kernel (A/B)")
+    ap.add_argument("--kubo", type=int, default=0, choices=[0, 3, 5],
+                    help="run only the Kubo leg of config 3 (sigma_xy) or 5 (sigma_xx)")
+    ap.add_argument("--cuda-core-mu", action="store_true", help="Kubo leg with the CUDA-core mu GEMM")
     ap.add_argument("--no-hopping", action="store_true",
                     help="diagonal-only H (same vector streams, no neighbour gathers): stream ceiling")
     args = ap.parse_args()
     if args.kernel_only:
         return run_kernel_only(args)
+    if args.kubo:
+        print(json.dumps(run_kubo(args.kubo, tensor=not args.cuda_core_mu)), flush=True)
+        return 0
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -231,6 +231,18 @@ enum { TBK_MU_CUDA_CORE = 0, TBK_MU_TENSOR = 1 };
 int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_sparse BR, int32_t M,
                 int32_t R, uint64_t seed, const double* kets, int32_t kernel_kind, double kp0,
                 double kp1, int32_t flags, double block_budget_gb, double* mu_out, void* stream);
+/* Device time of the last tbk_kubo_mu call in this process (CUDA events on its
+ * stream): building the stored blocks, the mu GEMM (+ split-K reduction), the
+ * real flops of the GEMM products issued (3 split-TF32 terms on the tensor
+ * path), the bytes of stored blocks written, and the number of vector chunks. */
+int tbk_kubo_last_timing(double* ms_blocks, double* ms_gemm, double* gemm_flops, double* block_bytes,
+                         int32_t* chunks);
+/* mu_mn = sum_k conj(L_m[k]) R_n[k] for given blocks (host, M x K complex128
+ * row-major each, rounded to complex64 on the device): the contraction of
+ * TB/snippets.h:337-342 on caller-supplied Chebyshev blocks.  flags: TBK_MU_*
+ * (TBK_MU_TENSOR: tcgen05 split-TF32 GEMM).  mu_out: host M x M complex128. */
+int tbk_mu_from_blocks(int32_t M, int64_t K, const double* L, const double* Rb, int32_t flags,
+                       double* mu_out, void* stream);
 /* zeta(e) = sum_mn mu_mn Gamma_mn(e) / (1-e^2)^2 / vol (FP64 on the device),
  * Gamma of TB/snippets.h:343-349; zeta_out: n_eps complex128. */
 int tbk_kubo_bastin_zeta(int32_t M, const double* mu, int32_t n_eps, const double* eps, double vol,

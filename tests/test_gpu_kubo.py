@@ -35,8 +35,9 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
+@pytest.mark.parametrize("tensor", [False, True])
 @pytest.mark.parametrize("which", ["bastin", "greenwood"])
-def test_mu_nm_vs_oracle(gpu, which):
+def test_mu_nm_vs_oracle(gpu, which, tensor):
     tb = gpu
     X, H = _system(tb)
     G = tb.GreenFunction(32, H, -4.1, 4.1)
@@ -47,10 +48,10 @@ def test_mu_nm_vs_oracle(gpu, which):
     kets = orc.random_phase_kets(n, 3, 2)
     g = orc.kernel_seq(orc.K_LORENTZ, 32, 6.0)
     if which == "bastin":
-        mu = tb.kubo_mu(Ht, None, None, v_x, v_y, M=32, kets=kets, kernel=tb.Lorentz(6.0))
+        mu = tb.kubo_mu(Ht, None, None, v_x, v_y, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=tensor)
         ref = orc.kubo_mu(n, cp, ri, v, 32, kets, AR=ovx, BR=ovy, g=g)
     else:
-        mu = tb.kubo_mu(Ht, v_x, v_x, None, None, M=32, kets=kets, kernel=tb.Lorentz(6.0))
+        mu = tb.kubo_mu(Ht, v_x, v_x, None, None, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=tensor)
         ref = orc.kubo_mu(n, cp, ri, v, 32, kets, AL=ovx, BL=ovx, g=g)
     assert _rel(mu, ref) <= MU_TOL, _rel(mu, ref)
 
@@ -90,12 +91,15 @@ def test_gamma_contractions_fp64(gpu):
     assert np.array_equal(E, Eo) and np.allclose(re, reo, rtol=1e-14, atol=0) and np.allclose(im, imo, rtol=1e-14, atol=0)
 
 
-def test_bastin_sigma_xy_end_to_end(gpu):
-    """conductivity_Kubo_Bastin (TB/snippets.h:306-456) vs the oracle pipeline."""
+@pytest.mark.parametrize("tensor", [False, True])
+def test_bastin_sigma_xy_end_to_end(gpu, tensor):
+    """conductivity_Kubo_Bastin (TB/snippets.h:306-456) vs the oracle pipeline;
+    stated bound: sigma_xy within 1e-5 of max |sigma| of the FP64 oracle."""
     tb = gpu
     X, H = _system(tb, (16, 16), flux=1 / 16)
     N, R = 64, 4
-    out = tb.conductivity_Kubo_Bastin(H, X.op_position(0), X.op_position(1), N, -4.0, 4.0, R=R, seed=2)
+    out = tb.conductivity_Kubo_Bastin(H, X.op_position(0), X.op_position(1), N, -4.0, 4.0, R=R, seed=2,
+                                      tensor=tensor)
     Ht = out["G"].scaled_HE
     n, cp, ri, v, ovx, ovy = _oracle_ops(tb, X, Ht)
     kets = orc.random_phase_kets(n, R, 2)

@@ -86,6 +86,8 @@ SIGNATURES = {
     "tbk_green_imag_fft": (C.c_int, [_i32, _vp, _vp, _i32, _vp, _vp, _vp]),
     "tbk_dos_from_moments": (C.c_int, [_i32, _vp, _i32, _d, _d, _d, _i32, _vp, _vp, _vp]),
     "tbk_kubo_mu": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _i32, _i32, _u64, _vp, _i32, _d, _d, _i32, _d, _vp, _vp]),
+    "tbk_kubo_last_timing": (C.c_int, [_pd, _pd, _pd, _pd, _pi32]),
+    "tbk_mu_from_blocks": (C.c_int, [_i32, _i64, _vp, _vp, _i32, _vp, _vp]),
     "tbk_kubo_bastin_zeta": (C.c_int, [_i32, _vp, _i32, _vp, _d, _vp, _vp]),
     "tbk_kubo_greenwood_sigma": (C.c_int, [_i32, _vp, _i32, _vp, _d, _vp, _vp]),
     "tbk_kubo_bastin_integrate": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _pi32]),

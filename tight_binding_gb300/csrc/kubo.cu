@@ -187,6 +187,15 @@ __global__ void greenwood_kernel(const double2* __restrict__ mu, int32_t M, cons
   }
 }
 
+__global__ void c128_to_c64_kernel(const double2* __restrict__ src, float2* __restrict__ dst, int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    dst[q] = make_float2(__double2float_rn(src[q].x), __double2float_rn(src[q].y));
+}
+
+// timing of the last tbk_kubo_mu call (CUDA events on the caller's stream)
+struct KuboTiming { double ms_blocks = 0, ms_gemm = 0, gemm_flops = 0, block_bytes = 0; int chunks = 0; };
+KuboTiming g_kubo_timing;
+
 int pick_chunk(int R) {
   int c = 1;
   while (c < R && c < 32) c <<= 1;
@@ -279,11 +288,16 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   const int64_t ksplit = 16384;
   const int32_t nsplit = (int32_t)((blk + ksplit - 1) / ksplit);
   if (!use_tc) TBK_TRY(part.alloc(sizeof(double2) * (size_t)nsplit * M * M));
+  cudaEvent_t ev[3];
+  for (auto& e : ev) TBK_CUDA(cudaEventCreate(&e));
+  KuboTiming tm;
   for (int32_t r0 = 0; r0 < R; r0 += Rc) {
+    TBK_CUDA(cudaEventRecord(ev[0], st));
     if (kets) TBK_TRY(load_block_any(true, n, R, r0, Rc, kstage.as<double2>(), v0, st));
     else TBK_TRY(random_block_any(true, n, R, r0, Rc, seed, v0, st));
     TBK_TRY(side(AL, BL, Ls.as<float2>()));
     TBK_TRY(side(AR, BR, Rs.as<float2>()));
+    TBK_CUDA(cudaEventRecord(ev[1], st));
     if (use_tc) {
       TBK_TRY(mu_gemm_tc(Ls.as<float2>(), Rs.as<float2>(), M, blk, blk, macc.as<double>(), st));
     } else {
@@ -294,7 +308,19 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
                                                                                        macc.as<double2>());
       TBK_CHECK_LAUNCH();
     }
+    TBK_CUDA(cudaEventRecord(ev[2], st));
+    TBK_CUDA(cudaEventSynchronize(ev[2]));
+    float a = 0.f, b = 0.f;
+    TBK_CUDA(cudaEventElapsedTime(&a, ev[0], ev[1]));
+    TBK_CUDA(cudaEventElapsedTime(&b, ev[1], ev[2]));
+    tm.ms_blocks += a;
+    tm.ms_gemm += b;
+    tm.gemm_flops += 8.0 * M * (double)M * (double)blk * (use_tc ? 3.0 : 1.0);   // real flops of the products issued
+    tm.block_bytes += 2.0 * M * (double)blk * 8.0;
+    tm.chunks += 1;
   }
+  for (auto& e : ev) cudaEventDestroy(e);
+  g_kubo_timing = tm;
   // kernel factors g_m g_n (FP64)
   std::vector<double> g(M);
   TBK_TRY(tbk_kernel_seq(kernel_kind, M, kp0, kp1, g.data()));
@@ -304,6 +330,56 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   TBK_CHECK_LAUNCH();
   TBK_CUDA(cudaMemcpyAsync(mu_out, macc.p, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, st));
   TBK_CUDA(cudaStreamSynchronize(st));
+  return TBK_OK;
+}
+
+int tbk_mu_from_blocks(int32_t M, int64_t K, const double* L, const double* Rb, int32_t flags, double* mu_out,
+                       void* stream) {
+  if (M < 1 || K < 1 || !L || !Rb || !mu_out) return fail(TBK_ERR_INVALID, "tbk_mu_from_blocks: bad argument");
+  cudaStream_t st = as_stream(stream);
+  const int64_t ld = K + (K & 1);                       // even stride keeps every block 16-byte aligned
+  const int64_t tot = (int64_t)M * K;
+  DevBuf stage, Ld, Rd, acc, part;
+  TBK_TRY(stage.alloc(sizeof(double2) * tot));
+  TBK_TRY(Ld.alloc(sizeof(float2) * M * ld));
+  TBK_TRY(Rd.alloc(sizeof(float2) * M * ld));
+  TBK_TRY(acc.alloc(sizeof(double2) * (size_t)M * M));
+  TBK_CUDA(cudaMemsetAsync(Ld.p, 0, Ld.bytes, st));
+  TBK_CUDA(cudaMemsetAsync(Rd.p, 0, Rd.bytes, st));
+  TBK_CUDA(cudaMemsetAsync(acc.p, 0, acc.bytes, st));
+  for (int side = 0; side < 2; ++side) {
+    TBK_CUDA(cudaMemcpyAsync(stage.p, side ? Rb : L, sizeof(double2) * tot, cudaMemcpyHostToDevice, st));
+    float2* dst = side ? Rd.as<float2>() : Ld.as<float2>();
+    for (int32_t m = 0; m < M; ++m) {
+      c128_to_c64_kernel<<<(unsigned)std::min<int64_t>((K + 255) / 256, 4096), 256, 0, st>>>(stage.as<double2>() + m * K,
+                                                                                            dst + m * ld, K);
+      TBK_CHECK_LAUNCH();
+    }
+  }
+  if (flags & TBK_MU_TENSOR) {
+    TBK_TRY(mu_gemm_tc(Ld.as<float2>(), Rd.as<float2>(), M, K, ld, acc.as<double>(), st));
+  } else {
+    const int64_t ksplit = 16384;
+    const int32_t nsplit = (int32_t)((K + ksplit - 1) / ksplit);
+    TBK_TRY(part.alloc(sizeof(double2) * (size_t)nsplit * M * M));
+    dim3 g((M + kGT - 1) / kGT, (M + kGT - 1) / kGT, nsplit);
+    mu_gemm_cc_kernel<<<g, 256, 0, st>>>(Ld.as<float2>(), Rd.as<float2>(), M, K, ld, ksplit, part.as<double2>());
+    TBK_CHECK_LAUNCH();
+    mu_split_reduce_kernel<<<(unsigned)(((int64_t)M * M + 255) / 256), 256, 0, st>>>(part.as<double2>(), M, nsplit,
+                                                                                     acc.as<double2>());
+    TBK_CHECK_LAUNCH();
+  }
+  TBK_CUDA(cudaMemcpyAsync(mu_out, acc.p, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  return TBK_OK;
+}
+
+int tbk_kubo_last_timing(double* ms_blocks, double* ms_gemm, double* gemm_flops, double* block_bytes, int32_t* chunks) {
+  if (ms_blocks) *ms_blocks = g_kubo_timing.ms_blocks;
+  if (ms_gemm) *ms_gemm = g_kubo_timing.ms_gemm;
+  if (gemm_flops) *gemm_flops = g_kubo_timing.gemm_flops;
+  if (block_bytes) *block_bytes = g_kubo_timing.block_bytes;
+  if (chunks) *chunks = g_kubo_timing.chunks;
   return TBK_OK;
 }
 

@@ -37,6 +37,25 @@ def kubo_mu(Ht: SparseMatrix, AL=None, BL=None, AR=None, BR=None, M: int = 64, R
     return mu
 
 
+def mu_from_blocks(L: np.ndarray, R: np.ndarray, tensor: bool = True) -> np.ndarray:
+    """mu_mn = sum_k conj(L[m, k]) R[n, k] on the GPU (blocks rounded to complex64)."""
+    L = np.ascontiguousarray(L, dtype=np.complex128)
+    R = np.ascontiguousarray(R, dtype=np.complex128)
+    M, K = L.shape
+    mu = np.zeros((M, M), dtype=np.complex128)
+    check(lib().tbk_mu_from_blocks(M, K, capi.ptr(L), capi.ptr(R), capi.MU_TENSOR if tensor else capi.MU_CUDA_CORE,
+                                   capi.ptr(mu), None))
+    return mu
+
+
+def kubo_last_timing() -> dict:
+    a, b, f, by = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+    n = C.c_int32()
+    check(lib().tbk_kubo_last_timing(C.byref(a), C.byref(b), C.byref(f), C.byref(by), C.byref(n)))
+    return {"ms_blocks": a.value, "ms_gemm": b.value, "gemm_flops": f.value, "block_bytes": by.value,
+            "chunks": n.value}
+
+
 def chebyshev_nodes(N: int) -> np.ndarray:
     """eps_k = cos((k + 1/2) pi / N), the nodes of the DCT-III (descending)."""
     return np.cos((np.arange(N) + 0.5) / N * math.pi)
