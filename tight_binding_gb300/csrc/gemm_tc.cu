@@ -119,10 +119,12 @@ __device__ __forceinline__ uint32_t plane_off(int row, int k, uint32_t lbo) {
   return (uint32_t)((k >> 2) * lbo + (row >> 3) * kSBO + (row & 7) * 16 + (k & 3) * 4);
 }
 
-// L, Rb: M blocks of ld complex64 (float2) each; the CTA covers rows m0.., n0..
-// and floats [kf0, kf1) of the interleaved K.  Writes FP64 partial tiles.
+// L, Rb: M blocks in the K-tiled layout (element k of block m at
+// ((k/16)*M + m)*16 + k%16, K padded with zeros to whole 16-element tiles); a
+// 32-float slab of 128 consecutive blocks is one contiguous 16 KB run.  The CTA
+// covers rows m0.., n0.. and floats [kf0, kf1).  Writes FP64 partial tiles.
 __global__ void __launch_bounds__(kThreads, 1) mu_tc_kernel(const float2* __restrict__ L, const float2* __restrict__ Rb,
-                                                            int32_t M, int64_t K, int64_t ld, int64_t kf_split,
+                                                            int32_t M, int64_t K, int64_t kf_split,
                                                             double* __restrict__ part_re, double* __restrict__ part_im,
                                                             int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -166,20 +168,15 @@ __global__ void __launch_bounds__(kThreads, 1) mu_tc_kernel(const float2* __rest
       if (!bar_wait(&empty_bar[st], ph ^ 1u)) { atomicOr(err, kErrEmpty); break; }
       unsigned char* sb = smem + (size_t)st * kStageBytes;
       const int64_t kf = kf0 + (int64_t)s * kKS;
-      // A row t: floats [kf, kf + 32) of block m0 + t
+      // A row t: the 32 floats of K-tile kf/32 of block m0 + t (consecutive threads
+      // read consecutive 128-byte rows: one coalesced 16 KB run per slab)
+      const int64_t tile = kf >> 5;
       {
         const int32_t m = m0 + t;
-        const float* src = reinterpret_cast<const float*>(L + (int64_t)m * ld);
+        const float4* src = reinterpret_cast<const float4*>(L + (tile * M + m) * 16);
 #pragma unroll
         for (int q = 0; q < kKS / 4; ++q) {
-          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-          const int64_t k = kf + 4 * q;
-          if (m < M && k + 3 < kf1) v = __ldcs(reinterpret_cast<const float4*>(src + k));
-          else if (m < M) {
-            float w[4] = {0.f, 0.f, 0.f, 0.f};
-            for (int e = 0; e < 4; ++e) if (k + e < kf1) w[e] = src[k + e];
-            v = make_float4(w[0], w[1], w[2], w[3]);
-          }
+          const float4 v = (m < M) ? __ldcs(src + q) : make_float4(0.f, 0.f, 0.f, 0.f);
           const float x[4] = {v.x, v.y, v.z, v.w};
           uint32_t hi[4], lo[4];
 #pragma unroll
@@ -192,17 +189,10 @@ __global__ void __launch_bounds__(kThreads, 1) mu_tc_kernel(const float2* __rest
       // B rows: t < 32 -> row t (R_n) and row 32 + t (pairs (im, -re))
       if (t < kTNc) {
         const int32_t n = n0 + t;
-        const float* src = reinterpret_cast<const float*>(Rb + (int64_t)n * ld);
+        const float4* src = reinterpret_cast<const float4*>(Rb + (tile * M + n) * 16);
 #pragma unroll
         for (int q = 0; q < kKS / 4; ++q) {
-          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-          const int64_t k = kf + 4 * q;
-          if (n < M && k + 3 < kf1) v = __ldcs(reinterpret_cast<const float4*>(src + k));
-          else if (n < M) {
-            float w[4] = {0.f, 0.f, 0.f, 0.f};
-            for (int e = 0; e < 4; ++e) if (k + e < kf1) w[e] = src[k + e];
-            v = make_float4(w[0], w[1], w[2], w[3]);
-          }
+          const float4 v = (n < M) ? __ldcs(src + q) : make_float4(0.f, 0.f, 0.f, 0.f);
           const float x[4] = {v.x, v.y, v.z, v.w};
           const float xp[4] = {v.y, -v.x, v.w, -v.z};      // (re, im) -> (im, -re)
           uint32_t hi[4], lo[4], hp[4], lp[4];
@@ -312,10 +302,9 @@ __global__ void mu_tc_reduce_kernel(const double* __restrict__ pr, const double*
 
 }  // namespace
 
-int mu_gemm_tc(const float2* L, const float2* Rb, int32_t M, int64_t K, int64_t ld, double* mu_acc, cudaStream_t st) {
+int mu_gemm_tc(const float2* L, const float2* Rb, int32_t M, int64_t K, double* mu_acc, cudaStream_t st) {
   if (M < 1 || K < 1) return fail(TBK_ERR_INVALID, "mu_gemm_tc: empty problem");
-  if (((uintptr_t)L | (uintptr_t)Rb) & 15 || (ld & 1))
-    return fail(TBK_ERR_INVALID, "mu_gemm_tc: blocks must be 16-byte aligned with an even stride");
+  if (((uintptr_t)L | (uintptr_t)Rb) & 15) return fail(TBK_ERR_INVALID, "mu_gemm_tc: blocks must be 16-byte aligned");
   static bool configured = false;
   if (!configured) {
     TBK_CUDA(cudaFuncSetAttribute(mu_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
@@ -335,7 +324,7 @@ int mu_gemm_tc(const float2* L, const float2* Rb, int32_t M, int64_t K, int64_t 
   TBK_TRY(errb.alloc(sizeof(int)));
   TBK_CUDA(cudaMemsetAsync(errb.p, 0, sizeof(int), st));
   dim3 grid(tiles, nsplit);
-  mu_tc_kernel<<<grid, kThreads, kSmemBytes, st>>>(L, Rb, M, K, ld, kf_split, pr.as<double>(), pi.as<double>(),
+  mu_tc_kernel<<<grid, kThreads, kSmemBytes, st>>>(L, Rb, M, K, kf_split, pr.as<double>(), pi.as<double>(),
                                                    errb.as<int>());
   TBK_CHECK_LAUNCH();
   mu_tc_reduce_kernel<<<(unsigned)(((int64_t)M * M + 255) / 256), 256, 0, st>>>(pr.as<double>(), pi.as<double>(), M,

@@ -7,7 +7,10 @@
 // generate_V_moments: as Greenwood with the Dirichlet kernel (TB/snippets.h:491-518)
 //
 // The stored blocks (Cheb_first_kind_seq_on_bases, TB/numerical.h:333-344) are
-// complex64 site-major blocks in HBM.  They are produced by the fused recursion
+// complex64 in HBM in a K-tiled layout: element k of block m lives at
+// ((k / 16) * M + m) * 16 + k % 16, so the 16-element K slab of any run of
+// consecutive blocks is contiguous (one coalesced 128-byte row per block) for
+// the mu GEMM.  They are produced by the fused recursion
 // step of kpm.cu running in complex128 on a three-block ring (the outer operator
 // AL/AR applied after each step), each stored value rounded to complex64 once.
 // Random vectors are processed in chunks so that both sides fit the block
@@ -24,13 +27,14 @@
 
 namespace tbk {
 
-int mu_gemm_tc(const float2* L, const float2* Rb, int32_t M, int64_t K, int64_t ldb, double* mu_acc,
-               cudaStream_t st);   // gemm_tc.cu (tensor cores, split TF32)
+int mu_gemm_tc(const float2* L, const float2* Rb, int32_t M, int64_t K, double* mu_acc,
+               cudaStream_t st);   // gemm_tc.cu (tensor cores, split TF32, K-tiled blocks)
 
 namespace {
 
 // ------------------------------------------------------------------ CUDA-core GEMM
-// C[m][n] += sum_k conj(L[m][k]) R[n][k] for a K range per CTA (split-K);
+// C[m][n] += sum_k conj(L[m][k]) R[n][k] for a K range per CTA (split-K), blocks
+// in the K-tiled layout;
 // FP32 products, FP32 sums over 32 terms promoted to FP64, FP64 partial tiles.
 constexpr int kGT = 32;      // output tile (complex) per CTA side
 constexpr int kGK = 32;      // K chunk staged in shared memory
@@ -50,8 +54,8 @@ __global__ void __launch_bounds__(256) mu_gemm_cc_kernel(const float2* __restric
       const int row = q / kGK, kk = q % kGK;
       const int64_t k = kb + kk;
       float2 z = make_float2(0.f, 0.f);
-      Ls[row][kk] = (m0 + row < M && k < k1) ? L[(int64_t)(m0 + row) * ld + k] : z;
-      Rs[row][kk] = (n0 + row < M && k < k1) ? Rb[(int64_t)(n0 + row) * ld + k] : z;
+      Ls[row][kk] = (m0 + row < M && k < k1) ? L[((k >> 4) * M + (m0 + row)) * 16 + (k & 15)] : z;
+      Rs[row][kk] = (n0 + row < M && k < k1) ? Rb[((k >> 4) * M + (n0 + row)) * 16 + (k & 15)] : z;
     }
     __syncthreads();
 #pragma unroll 8
@@ -95,10 +99,12 @@ __global__ void mu_split_reduce_kernel(const double2* __restrict__ part, int32_t
   acc[q].y += i;
 }
 
-// complex128 work block -> complex64 stored block (one rounding per element)
-__global__ void round_block_kernel(const double2* __restrict__ src, float2* __restrict__ dst, int64_t n) {
+// complex128 work block -> block m of the complex64 K-tiled store (one rounding
+// per element); 16 consecutive k form one contiguous 128-byte row of the tile
+__global__ void round_block_kernel(const double2* __restrict__ src, float2* __restrict__ store, int32_t m, int32_t M,
+                                   int64_t n) {
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-    dst[q] = make_float2(__double2float_rn(src[q].x), __double2float_rn(src[q].y));
+    store[((q >> 4) * M + m) * 16 + (q & 15)] = make_float2(__double2float_rn(src[q].x), __double2float_rn(src[q].y));
 }
 
 __global__ void mu_kernel_scale_kernel(double2* __restrict__ mu, const double* __restrict__ g, int32_t M) {
@@ -187,10 +193,7 @@ __global__ void greenwood_kernel(const double2* __restrict__ mu, int32_t M, cons
   }
 }
 
-__global__ void c128_to_c64_kernel(const double2* __restrict__ src, float2* __restrict__ dst, int64_t n) {
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-    dst[q] = make_float2(__double2float_rn(src[q].x), __double2float_rn(src[q].y));
-}
+
 
 // timing of the last tbk_kubo_mu call (CUDA events on the caller's stream)
 struct KuboTiming { double ms_blocks = 0, ms_gemm = 0, gemm_flops = 0, block_bytes = 0; int chunks = 0; };
@@ -236,8 +239,9 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   // edges, where the Kubo weights 1/(1-e^2)^2 are largest; each stored value is
   // rounded to complex64 exactly once)
   DevBuf Ls, Rs, work, partd, part, macc, gdev, kstage;
-  TBK_TRY(Ls.alloc(sizeof(float2) * blk * M));
-  TBK_TRY(Rs.alloc(sizeof(float2) * blk * M));
+  const int64_t blk16 = (blk + 15) / 16 * 16;           // K padded to whole 16-element tiles (zeros)
+  TBK_TRY(Ls.alloc(sizeof(float2) * blk16 * M));
+  TBK_TRY(Rs.alloc(sizeof(float2) * blk16 * M));
   TBK_TRY(work.alloc(sizeof(double2) * blk * 6));
   TBK_CUDA(cudaMemsetAsync(Ls.p, 0, Ls.bytes, st));
   TBK_CUDA(cudaMemsetAsync(Rs.p, 0, Rs.bytes, st));
@@ -261,8 +265,8 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     TBK_TRY(step_config(A, Rc, true, &g, &t, st));
     return step_any(A, Rc, true, x, y, nullptr, true, partd.as<double>(), g, t, st);
   };
-  auto round_to = [&](const double2* src, float2* dst) -> int {
-    round_block_kernel<<<(unsigned)std::min<int64_t>((blk + 255) / 256, 65535), 256, 0, st>>>(src, dst, blk);
+  auto round_to = [&](const double2* src, float2* store, int32_t m) -> int {
+    round_block_kernel<<<(unsigned)std::min<int64_t>((blk + 255) / 256, 65535), 256, 0, st>>>(src, store, m, M, blk);
     TBK_CHECK_LAUNCH();
     return TBK_OK;
   };
@@ -279,8 +283,8 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
         const double2* pv = m >= 2 ? r[(m - 2) % 3] : nullptr;
         TBK_TRY(step_any(Ht, Rc, true, x, y, pv, m == 1, partd.as<double>(), grid, n_tiles, st));
       }
-      if (Aout) { TBK_TRY(apply(Aout, y, tmpA)); TBK_TRY(round_to(tmpA, store + (int64_t)m * blk)); }
-      else TBK_TRY(round_to(y, store + (int64_t)m * blk));
+      if (Aout) { TBK_TRY(apply(Aout, y, tmpA)); TBK_TRY(round_to(tmpA, store, m)); }
+      else TBK_TRY(round_to(y, store, m));
     }
     return TBK_OK;
   };
@@ -299,7 +303,7 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     TBK_TRY(side(AR, BR, Rs.as<float2>()));
     TBK_CUDA(cudaEventRecord(ev[1], st));
     if (use_tc) {
-      TBK_TRY(mu_gemm_tc(Ls.as<float2>(), Rs.as<float2>(), M, blk, blk, macc.as<double>(), st));
+      TBK_TRY(mu_gemm_tc(Ls.as<float2>(), Rs.as<float2>(), M, blk, macc.as<double>(), st));
     } else {
       dim3 g((M + kGT - 1) / kGT, (M + kGT - 1) / kGT, nsplit);
       mu_gemm_cc_kernel<<<g, 256, 0, st>>>(Ls.as<float2>(), Rs.as<float2>(), M, blk, blk, ksplit, part.as<double2>());
@@ -337,33 +341,33 @@ int tbk_mu_from_blocks(int32_t M, int64_t K, const double* L, const double* Rb, 
                        void* stream) {
   if (M < 1 || K < 1 || !L || !Rb || !mu_out) return fail(TBK_ERR_INVALID, "tbk_mu_from_blocks: bad argument");
   cudaStream_t st = as_stream(stream);
-  const int64_t ld = K + (K & 1);                       // even stride keeps every block 16-byte aligned
-  const int64_t tot = (int64_t)M * K;
+  const int64_t K16 = (K + 15) / 16 * 16;
   DevBuf stage, Ld, Rd, acc, part;
-  TBK_TRY(stage.alloc(sizeof(double2) * tot));
-  TBK_TRY(Ld.alloc(sizeof(float2) * M * ld));
-  TBK_TRY(Rd.alloc(sizeof(float2) * M * ld));
+  TBK_TRY(stage.alloc(sizeof(double2) * K));
+  TBK_TRY(Ld.alloc(sizeof(float2) * M * K16));
+  TBK_TRY(Rd.alloc(sizeof(float2) * M * K16));
   TBK_TRY(acc.alloc(sizeof(double2) * (size_t)M * M));
   TBK_CUDA(cudaMemsetAsync(Ld.p, 0, Ld.bytes, st));
   TBK_CUDA(cudaMemsetAsync(Rd.p, 0, Rd.bytes, st));
   TBK_CUDA(cudaMemsetAsync(acc.p, 0, acc.bytes, st));
   for (int side = 0; side < 2; ++side) {
-    TBK_CUDA(cudaMemcpyAsync(stage.p, side ? Rb : L, sizeof(double2) * tot, cudaMemcpyHostToDevice, st));
     float2* dst = side ? Rd.as<float2>() : Ld.as<float2>();
+    const double* src = side ? Rb : L;
     for (int32_t m = 0; m < M; ++m) {
-      c128_to_c64_kernel<<<(unsigned)std::min<int64_t>((K + 255) / 256, 4096), 256, 0, st>>>(stage.as<double2>() + m * K,
-                                                                                            dst + m * ld, K);
+      TBK_CUDA(cudaMemcpyAsync(stage.p, src + 2 * (int64_t)m * K, sizeof(double2) * K, cudaMemcpyHostToDevice, st));
+      round_block_kernel<<<(unsigned)std::min<int64_t>((K + 255) / 256, 4096), 256, 0, st>>>(stage.as<double2>(), dst, m,
+                                                                                          M, K);
       TBK_CHECK_LAUNCH();
     }
   }
   if (flags & TBK_MU_TENSOR) {
-    TBK_TRY(mu_gemm_tc(Ld.as<float2>(), Rd.as<float2>(), M, K, ld, acc.as<double>(), st));
+    TBK_TRY(mu_gemm_tc(Ld.as<float2>(), Rd.as<float2>(), M, K, acc.as<double>(), st));
   } else {
     const int64_t ksplit = 16384;
     const int32_t nsplit = (int32_t)((K + ksplit - 1) / ksplit);
     TBK_TRY(part.alloc(sizeof(double2) * (size_t)nsplit * M * M));
     dim3 g((M + kGT - 1) / kGT, (M + kGT - 1) / kGT, nsplit);
-    mu_gemm_cc_kernel<<<g, 256, 0, st>>>(Ld.as<float2>(), Rd.as<float2>(), M, K, ld, ksplit, part.as<double2>());
+    mu_gemm_cc_kernel<<<g, 256, 0, st>>>(Ld.as<float2>(), Rd.as<float2>(), M, K, 0, ksplit, part.as<double2>());
     TBK_CHECK_LAUNCH();
     mu_split_reduce_kernel<<<(unsigned)(((int64_t)M * M + 255) / 256), 256, 0, st>>>(part.as<double2>(), M, nsplit,
                                                                                      acc.as<double2>());
