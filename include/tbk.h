@@ -258,6 +258,76 @@ int tbk_kubo_bastin_integrate(int32_t N, const double* eps, const double* zeta, 
                               double* re_out, double* im_out, int32_t* n_out);
 
 /* =========================================================================
+ * Serving: many density-of-states solves advanced together.  No counterpart in
+ * the reference, which runs one solve per call (density_of_states_seq,
+ * TB/functions.h:15-32, over the moments of TB/numerics_cuda.cu:190-255).
+ *
+ * A request is a lattice spec plus spectral bounds, M, R, seed and precision.
+ * The server copies it at submit, admits it in FIFO order against an HBM
+ * budget, builds H~ = (H - b)/a on the device (TBK_BUILD_* as for
+ * tbk_build_hamiltonian, a = (e_max - e_min)/2, b = (e_max + e_min)/2) and then
+ * advances the running requests together: each round runs `steps_per_round`
+ * doubling recursion steps, one launch per (precision, vector width) group and
+ * step, packed over all of the group's requests, captured once per group set
+ * as a CUDA graph.  Built requests join the running set between rounds while
+ * the bytes one step moves stay under `step_gb`.  The random-phase kets are those of tbk_kpm_run_random(seed)
+ * and the result is mu_0 .. mu_{M-1} as tbk_kpm_run_random computes them with
+ * TBK_FLAG_DOUBLING.  A request's moments do not depend on what else is
+ * resident: its sums run in an order fixed by its own size, so a request gives
+ * the same bits alone and in any mix.
+ * ========================================================================= */
+enum { TBK_PENDING = 7 };            /* tbk_server_poll: not finished yet         */
+typedef struct tbk_server_s* tbk_server;
+typedef struct {
+  double budget_gb;                  /* HBM admission cap (<= 0: 120 GB)          */
+  int32_t steps_per_round;           /* recursion steps per round (<= 0: 16)      */
+  int32_t autotune;                  /* 1: time launch shapes per group at create */
+  int32_t max_resident;              /* cap on resident requests (<= 0: 4096)     */
+  int32_t result_arena_mb;           /* pinned result arena in MiB (<= 0: 64)     */
+  double step_gb;                    /* running set: join built requests while the
+                                        bytes one step moves stay below this (<= 0:
+                                        2 GB; one request always runs)            */
+} tbk_server_config;
+typedef struct {
+  tbk_lattice lattice;               /* copied at submit                          */
+  int32_t build_mode;                /* TBK_BUILD_*                               */
+  int32_t extend[3];                 /* periodic axes (TBK_BUILD_PERIODIC_BARE)   */
+  int32_t is_complex;                /* Scalar of H (0: double, 1: complex)       */
+  int32_t n_mom;                     /* M >= 2                                    */
+  int32_t R;                         /* random-phase vectors >= 1                 */
+  int32_t precision;                 /* TBK_PREC_MIXED or TBK_PREC_FP64           */
+  uint64_t seed;
+  double e_min, e_max;               /* spectral bounds of H (e_max > e_min)      */
+} tbk_request;
+int tbk_server_create(tbk_server* out, const tbk_server_config* cfg);
+/* Stops admitting, lets the rounds in flight end, fails what is still queued
+ * or resident, frees everything. */
+void tbk_server_destroy(tbk_server server);
+/* Queues a request; *ticket identifies it.  TBK_ERR_BUDGET when its build peak
+ * alone exceeds the budget. */
+int tbk_server_submit(tbk_server server, const tbk_request* req, int64_t* ticket);
+/* Waits up to wait_ms (>= 0) for the request.  Done: copies the n_mom moments
+ * to mu_out, times_ms[4] = {queued, build, resident, total} (may be NULL),
+ * forgets the ticket and returns TBK_OK.  Not done: TBK_PENDING.  Failed: its
+ * status (and forgets the ticket). */
+int tbk_server_poll(tbk_server server, int64_t ticket, int32_t wait_ms, double* mu_out,
+                    double* times_ms);
+/* Footprint of a request as admission charges it: build peak and resident
+ * bytes (host arithmetic, no device needed). */
+int tbk_request_footprint(const tbk_request* req, int64_t* build_peak_bytes,
+                          int64_t* resident_bytes);
+/* Counters, out[0 .. n-1] in this order: requests done, failed, rounds, graphs
+ * instantiated, GPU busy ms (sum of round durations), algorithmic bytes moved,
+ * site-vector updates, step launches, budget bytes, peak reserved bytes,
+ * reserved bytes now, build ms (sum), peak resident requests, build overshoot
+ * bytes (max over builds of pool high-water minus reservation; <= 0 when
+ * admission charged enough). */
+int tbk_server_stats(tbk_server server, double* out, int32_t n);
+/* Launch shape chosen per group, rows[5*i ..] = {precision, width, grid,
+ * prefetch distance, ms per step}; returns the number of rows written. */
+int tbk_server_tuning(tbk_server server, int32_t max_rows, double* rows);
+
+/* =========================================================================
  * Chebyshev moments without device allocation.  No counterpart in the
  * reference: it serves callers that may not allocate GPU memory while they run
  * (a fixed, fully reserved HBM budget; a host that lends device buffers but

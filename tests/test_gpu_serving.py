@@ -1,0 +1,155 @@
+"""Serving loop on the GPU: every request against the FP64 oracle on the same
+seeded kets, the same bits alone and in a mix, and admission under a budget.
+
+Tolerances (relative to mu_0, as for the single-solve moments):
+  FP64 requests   <= 1e-10
+  mixed requests  <= MIXED_TOL (M <= 256)"""
+import numpy as np
+import pytest
+
+import oracle as orc
+from serving_cases import bounds, cell, lattice
+
+pytestmark = pytest.mark.gpu
+MIXED_TOL = 2e-5
+
+
+def _oracle(tb, X, n_mom, R, seed, emin, emax):
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1] * X.dim, float)
+    G = tb.GreenFunction(8, H, emin, emax)
+    cp, ri, v = G.scaled_HE.to_csc()
+    n = len(cp) - 1
+    kets = orc.random_phase_kets(n, R, seed)
+    return orc.cheb_moments(n, cp, ri, v, n_mom, kets, kets)
+
+
+def _err(mu, ref):
+    return float(np.max(np.abs(mu - ref)) / abs(ref[0]))
+
+
+CASES = [  # kind, L, W, M, R, precision
+    ("square", 24, 1.0, 128, 4, "mixed"),
+    ("honeycomb", 16, 0.5, 64, 8, "fp64"),
+    ("kagome", 12, 2.0, 96, 5, "mixed"),
+    ("lieb", 12, 0.0, 80, 64, "fp64"),
+    ("fcc", 8, 1.5, 201, 16, "mixed"),
+    ("square", 10, 0.3, 2, 3, "fp64"),
+    ("honeycomb", 20, 1.2, 256, 64, "mixed"),
+]
+
+
+def test_requests_vs_oracle(gpu):
+    tb = gpu
+    with tb.DosServer(autotune=True, steps_per_round=8) as srv:
+        tickets = []
+        for i, (kind, L, W, M, R, prec) in enumerate(CASES):
+            X = lattice(tb, kind, L, W, seed=100 + i)
+            emin, emax = bounds(kind, W)
+            tickets.append(srv.submit(X, M, R, seed=i, e_min=emin, e_max=emax, precision=prec))
+        for i, (kind, L, W, M, R, prec) in enumerate(CASES):
+            mu, times = srv.result(tickets[i], timeout_s=120)
+            X = lattice(tb, kind, L, W, seed=100 + i)
+            ref = _oracle(tb, X, M, R, i, *bounds(kind, W))
+            tol = 1e-10 if prec == "fp64" else MIXED_TOL
+            assert _err(mu, ref) <= tol, (kind, prec, _err(mu, ref))
+            assert abs(mu[0] - R) < 1e-4 * R
+            assert times[3] >= times[2] >= 0
+        st = srv.stats()
+        assert st["done"] == len(CASES) and st["failed"] == 0
+        assert st["reserved_bytes"] == 0
+        assert len(srv.tuning()) == 9
+
+
+def _mix(tb, cells):
+    out = []
+    kinds = ["square", "honeycomb", "kagome", "lieb", "fcc"]
+    rng = np.random.default_rng(5)
+    for i in range(12):
+        kind = kinds[i % 5]
+        L = int(rng.integers(8, 14)) if kind == "fcc" else int(rng.integers(16, 72))
+        W = float(rng.uniform(0, 2))
+        out.append(dict(kind=kind, L=L, W=W, M=int(rng.choice([64, 128, 256])), R=int(rng.choice([4, 8, 16, 32, 64])),
+                        prec="fp64" if i % 3 == 0 else "mixed", seed=200 + i))
+    return out
+
+
+def _submit(tb, srv, c, cells):
+    X = lattice(tb, c["kind"], c["L"], c["W"], seed=c["seed"], cells=cells)
+    emin, emax = bounds(c["kind"], c["W"])
+    return srv.submit(X, c["M"], c["R"], seed=c["seed"], e_min=emin, e_max=emax, precision=c["prec"])
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_alone_equals_in_mix(gpu, prec):
+    """A request's moments are the same bits alone, in a mix of other lattices,
+    widths and precisions, and with another round length and launch shape."""
+    tb = gpu
+    cells = {k: cell(tb, k) for k in ("square", "honeycomb", "kagome", "lieb", "fcc")}
+    probe = dict(kind="honeycomb", L=48, W=1.3, M=200, R=16, prec=prec, seed=77)
+    with tb.DosServer(autotune=True, steps_per_round=16) as srv:
+        alone, _ = srv.result(_submit(tb, srv, probe, cells))
+        mix = _mix(tb, cells)
+        tickets = [_submit(tb, srv, c, cells) for c in mix[:6]]
+        t_probe = _submit(tb, srv, probe, cells)
+        tickets += [_submit(tb, srv, c, cells) for c in mix[6:]]
+        in_mix, _ = srv.result(t_probe)
+        for t in tickets:
+            srv.result(t)
+        assert srv.stats()["peak_resident"] > 1
+    assert np.array_equal(alone, in_mix)
+    with tb.DosServer(autotune=False, steps_per_round=4) as srv2:
+        other, _ = srv2.result(_submit(tb, srv2, probe, cells))
+    assert np.array_equal(alone, other)
+
+
+def test_budget_admission(gpu):
+    tb = gpu
+    X = lattice(tb, "square", 96, 1.0, seed=1)
+    emin, emax = bounds("square", 1.0)
+    peak, res = tb.request_footprint(X, 128, 32, "mixed", emin, emax)
+    # room for one build peak plus half of one request's vector blocks: a
+    # resident request (which holds all of its blocks) and a second build never fit
+    budget = peak + 96 * 96 * 32 * 8
+    with tb.DosServer(budget_gb=budget / 1e9, autotune=False) as srv:
+        ts = [srv.submit(X, 128, 32, seed=s, e_min=emin, e_max=emax) for s in range(5)]
+        mus = [srv.result(t)[0] for t in ts]
+        st = srv.stats()
+        assert st["done"] == 5
+        assert st["peak_reserved_bytes"] <= budget
+        assert st["peak_resident"] == 1          # one build peak fits, two do not
+        assert st["build_overshoot_bytes"] <= 0  # the pool never held more than was charged
+        big = lattice(tb, "square", 400)
+        with pytest.raises(tb.TbkError) as e:
+            srv.submit(big, 128, 64, seed=0, e_min=emin, e_max=emax)
+        assert e.value.code == tb.capi.TBK_ERR_BUDGET
+    # different seeds, different moments; the same seed alone reproduces
+    assert not np.array_equal(mus[0], mus[1])
+    ref = _oracle(tb, X, 128, 32, 3, emin, emax)
+    assert _err(mus[3], ref) <= MIXED_TOL
+
+
+def test_many_small_requests_packed(gpu):
+    tb = gpu
+    cells = {"square": cell(tb, "square")}
+    with tb.DosServer(autotune=False, steps_per_round=16) as srv:
+        ts = [_submit(tb, srv, dict(kind="square", L=8 + (i % 24), W=0.5, M=64, R=4, prec="mixed", seed=i), cells)
+              for i in range(96)]
+        res = [srv.result(t)[0] for t in ts]
+        st = srv.stats()
+    assert st["done"] == 96
+    # 33 steps each: 3 rounds alone; packed, fewer rounds than one after another
+    assert st["rounds"] < 3 * 96
+    assert st["peak_resident"] > 1
+    for i in (0, 37, 95):
+        X = lattice(tb, "square", 8 + (i % 24), 0.5, seed=i)
+        ref = _oracle(tb, X, 64, 4, i, *bounds("square", 0.5))
+        assert _err(res[i], ref) <= MIXED_TOL
+
+
+def test_poll_unknown_ticket(gpu):
+    tb = gpu
+    with tb.DosServer(autotune=False) as srv:
+        with pytest.raises(KeyError):
+            srv.poll(12345)
+        import ctypes as C
+        assert tb.capi.lib().tbk_server_poll(srv._h, 12345, 0, None, None) == tb.capi.TBK_ERR_INVALID

@@ -12,5 +12,6 @@ from .kubo import (bastin_integrate, bastin_zeta, chebyshev_nodes, conductivity_
 from .kpm import (Cheb_first_kind_seq_braket, Dirichlet, Fejer, GreenFunction, GreenFunctionImag, Jackson,
                   KpmSolver, Kernel, Lanczos, Lorentz, Wang_and_Zunger, bases_of_uniform_ampl_with_random_phases,
                   density_of_states_function, density_of_states_seq, dos_from_moments, kernel_seq)
+from .serving import DosServer, request_footprint
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -21,6 +21,7 @@ TBK_ERR_NOMEM = 3
 TBK_ERR_UNSUPPORTED = 4
 TBK_ERR_TIMEOUT = 5
 TBK_ERR_BUDGET = 6
+TBK_PENDING = 7
 
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -39,6 +40,22 @@ KERNEL_DIRICHLET, KERNEL_FEJER, KERNEL_LORENTZ, KERNEL_JACKSON, KERNEL_LANCZOS, 
 
 _i32, _i64, _u64, _d, _vp, _cp = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_void_p, C.c_char_p
 _pi32, _pi64, _pd, _pu8 = C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_uint8)
+
+
+class ServerConfig(C.Structure):
+    """tbk_server_config"""
+    _fields_ = [("budget_gb", C.c_double), ("steps_per_round", C.c_int32), ("autotune", C.c_int32),
+                ("max_resident", C.c_int32), ("result_arena_mb", C.c_int32), ("step_gb", C.c_double)]
+
+
+class Request(C.Structure):
+    """tbk_request"""
+    _fields_ = [("lattice", C.c_void_p), ("build_mode", C.c_int32), ("extend", C.c_int32 * 3),
+                ("is_complex", C.c_int32), ("n_mom", C.c_int32), ("R", C.c_int32), ("precision", C.c_int32),
+                ("seed", C.c_uint64), ("e_min", C.c_double), ("e_max", C.c_double)]
+
+
+_pcfg, _preq = C.POINTER(ServerConfig), C.POINTER(Request)
 
 # name -> (restype, argtypes); every function declared in include/tbk.h
 SIGNATURES = {
@@ -91,6 +108,13 @@ SIGNATURES = {
     "tbk_kubo_bastin_zeta": (C.c_int, [_i32, _vp, _i32, _vp, _d, _vp, _vp]),
     "tbk_kubo_greenwood_sigma": (C.c_int, [_i32, _vp, _i32, _vp, _d, _vp, _vp]),
     "tbk_kubo_bastin_integrate": (C.c_int, [_i32, _vp, _vp, _vp, _vp, _vp, _pi32]),
+    "tbk_server_create": (C.c_int, [C.POINTER(_vp), _pcfg]),
+    "tbk_server_destroy": (None, [_vp]),
+    "tbk_server_submit": (C.c_int, [_vp, _preq, _pi64]),
+    "tbk_server_poll": (C.c_int, [_vp, _i64, _i32, _vp, _vp]),
+    "tbk_request_footprint": (C.c_int, [_preq, _pi64, _pi64]),
+    "tbk_server_stats": (C.c_int, [_vp, _vp, _i32]),
+    "tbk_server_tuning": (C.c_int, [_vp, _i32, _vp]),
     "tbk_cheb_moments_noalloc": (C.c_int, [_i32, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _i32, _vp, _vp]),
 }
 

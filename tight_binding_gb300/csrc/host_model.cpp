@@ -22,6 +22,7 @@ namespace tbk {
 
 static thread_local std::string g_last_error;
 static thread_local int g_last_code = 0;
+thread_local const AsyncAllocCtx* tl_async_alloc = nullptr;
 
 void set_error(int code, const std::string& msg) { g_last_code = code; g_last_error = msg; }
 

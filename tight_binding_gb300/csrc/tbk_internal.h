@@ -30,25 +30,51 @@ int fail(int code, const char* fmt, ...);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
-// ---- device buffer (RAII, cudaMalloc)
+// ---- stream-ordered allocation context.  While a thread has one installed,
+// DevBuf takes its memory from the context's pool on the context's stream and
+// gives it back with cudaFreeAsync, so that freeing never waits for the device.
+struct AsyncAllocCtx {
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t stream = nullptr;
+};
+extern thread_local const AsyncAllocCtx* tl_async_alloc;
+
+// ---- device buffer (RAII, cudaMalloc or the thread's stream-ordered pool)
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  const AsyncAllocCtx* ctx = nullptr;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
-  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes), ctx(o.ctx) { o.p = nullptr; o.bytes = 0; o.ctx = nullptr; }
   DevBuf& operator=(DevBuf&& o) noexcept {
-    if (this != &o) { release(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+    if (this != &o) {
+      release();
+      p = o.p; bytes = o.bytes; ctx = o.ctx;
+      o.p = nullptr; o.bytes = 0; o.ctx = nullptr;
+    }
     return *this;
   }
   ~DevBuf() { release(); }
-  void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
+  void release() {
+    if (p) {
+      if (ctx) cudaFreeAsync(p, ctx->stream);
+      else cudaFree(p);
+    }
+    p = nullptr; bytes = 0; ctx = nullptr;
+  }
   int alloc(size_t n) {
     release();
     if (n == 0) n = 16;
-    cudaError_t e = cudaMalloc(&p, n);
-    if (e != cudaSuccess) { p = nullptr; return fail(TBK_ERR_NOMEM, "cudaMalloc(%zu): %s", n, cudaGetErrorString(e)); }
+    cudaError_t e;
+    if (tl_async_alloc) {
+      e = cudaMallocFromPoolAsync(&p, n, tl_async_alloc->pool, tl_async_alloc->stream);
+      if (e == cudaSuccess) ctx = tl_async_alloc;
+    } else {
+      e = cudaMalloc(&p, n);
+    }
+    if (e != cudaSuccess) { p = nullptr; return fail(TBK_ERR_NOMEM, "device allocation of %zu bytes: %s", n, cudaGetErrorString(e)); }
     bytes = n;
     return TBK_OK;
   }
