@@ -404,6 +404,124 @@ def run_kubo(config: int, tensor: bool = True):
     return line
 
 
+SERVE_KINDS = ("square", "honeycomb", "kagome", "lieb", "fcc")
+
+
+def serve_stream(n: int, gap_ms: float, seed: int = 3):
+    """The serving workload: Poisson arrivals (mean gap gap_ms), lattice kind
+    uniform over SERVE_KINDS, linear size U{32..512} (2D) or U{16..64} (FCC),
+    disorder W ~ U[0, 2], M in {256, 512, 1024}, R in {4, 8, 16, 32, 64}."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(gap_ms, n)
+    arrive = np.cumsum(gaps) - gaps[0]
+    kind = rng.integers(0, len(SERVE_KINDS), n)
+    L2 = rng.integers(32, 513, n)
+    L3 = rng.integers(16, 65, n)
+    W = rng.uniform(0.0, 2.0, n)
+    M = rng.choice([256, 512, 1024], n)
+    R = rng.choice([4, 8, 16, 32, 64], n)
+    out = []
+    for i in range(n):
+        k = SERVE_KINDS[kind[i]]
+        out.append(dict(t_ms=float(arrive[i]), kind=k, L=int(L3[i] if k == "fcc" else L2[i]), W=float(W[i]),
+                        M=int(M[i]), R=int(R[i]), seed=i))
+    return out
+
+
+def run_serve(args):
+    """Config 4: a stream of DoS requests through the continuous-batching server
+    (admission under the HBM budget, graph-captured rounds packed over all
+    running requests).  value = requests/s over the whole stream; latency =
+    submit -> result per request."""
+    import tight_binding_gb300 as tb
+    from tight_binding_gb300.serving import model_bounds, model_cell
+
+    ws, rank, local = dist_info()
+    reqs = serve_stream(args.serve_requests, args.serve_gap_ms)
+    # weak scaling over ranks: rank r serves requests r, r + ws, ...
+    mine = reqs[rank::ws]
+    cells = {k: model_cell(k) for k in SERVE_KINDS}
+    srv = tb.DosServer(budget_gb=args.serve_budget_gb, steps_per_round=args.serve_round, autotune=True,
+                       step_gb=args.serve_step_gb)
+    tuning = srv.tuning()
+    tickets = [None] * len(mine)
+    ready = threading.Semaphore(0)
+    err = []
+
+    def lat(q):
+        span = (q["L"],) * (3 if q["kind"] == "fcc" else 2)
+        X = tb.PartialLattice(cells[q["kind"]], span)
+        if q["W"] > 0:
+            X.set_scalar_disorder(q["W"], q["seed"])
+        return X
+
+    def submitter():
+        t0 = time.perf_counter()
+        try:
+            for i, q in enumerate(mine):
+                dt = q["t_ms"] / 1e3 - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                emin, emax = model_bounds(q["kind"], q["W"])
+                tickets[i] = srv.submit(lat(q), q["M"], q["R"], seed=q["seed"], e_min=emin, e_max=emax,
+                                        precision=args.serve_precision)
+                ready.release()
+        except Exception as e:          # surfaced by the main thread
+            err.append(e)
+            ready.release()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    t_start = time.perf_counter()
+    th = threading.Thread(target=submitter, daemon=True)
+    th.start()
+    lat_ms, queued_ms, build_ms, bad = [], [], [], 0
+    for i in range(len(mine)):
+        ready.acquire()
+        if err:
+            raise err[0]
+        mu, times = srv.result(tickets[i], timeout_s=1800)
+        q = mine[i]
+        if not (np.all(np.isfinite(mu)) and abs(mu[0] - q["R"]) < 1e-3 * q["R"]):
+            bad += 1
+        lat_ms.append(times[3])
+        queued_ms.append(times[0])
+        build_ms.append(times[1])
+    wall = time.perf_counter() - t_start
+    th.join()
+    clocks = sampler.stop()
+    st = srv.stats()
+    srv.close()
+    peak, peak_kind = peaks()
+    achieved = st["bytes"] / (st["busy_ms"] / 1e3) / 1e9 if st["busy_ms"] > 0 else 0.0
+    line = {
+        "metric": "DoS serving stream: requests/s and p50/p99 latency (submit -> moments)",
+        "value": len(mine) / wall, "unit": "requests/s",
+        "n_gpus": ws, "steps": len(mine), "warmup": 0, "ms_per_step": 1e3 * wall / len(mine),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64" if args.serve_precision == "mixed" else "c128", "data": "synthetic",
+        "config": {"workload": f"{args.serve_requests} DoS requests, Poisson arrivals mean gap "
+                               f"{args.serve_gap_ms} ms (seed 3); square/honeycomb/Kagome/Lieb L~U{{32..512}}, "
+                               f"FCC L~U{{16..64}}; NN t=1.0 + disorder W~U[0,2]; M in {{256,512,1024}}; "
+                               f"R in {{4,8,16,32,64}}; {args.serve_precision} recursion (doubling)",
+                   "budget_gb": args.serve_budget_gb, "steps_per_round": args.serve_round,
+                   "step_gb": args.serve_step_gb, "l2": "resident working set far above L2; no flush"},
+        "updates_per_s": st["updates"] / wall,
+        "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
+                       "mean": float(np.mean(lat_ms)), "max": float(np.max(lat_ms)),
+                       "queued_p50": float(np.percentile(queued_ms, 50)),
+                       "build_p50": float(np.percentile(build_ms, 50))},
+        "wall_s": wall, "gpu_busy_frac": st["busy_ms"] / 1e3 / wall,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "kernel": "srv_step_kernel (all groups, over GPU-busy time)"},
+        "gpu_launches": int(st["launches"]), "server": st, "tuning": tuning, "bad_results": bad, "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_kernel_only(args):
     """Small case of the same kernel for ncu captures: one mixed-precision DoS
     solve (doubling) on a honeycomb of --cells^2 cells, R = 32."""
@@ -446,7 +564,16 @@ def main():
     ap.add_argument("--cuda-core-mu", action="store_true", help="Kubo leg with the CUDA-core mu GEMM")
     ap.add_argument("--no-hopping", action="store_true",
                     help="diagonal-only H (same vector streams, no neighbour gathers): stream ceiling")
+    ap.add_argument("--serve", action="store_true", help="serving stream (config 4) instead of the DoS solve")
+    ap.add_argument("--serve-requests", type=int, default=4096)
+    ap.add_argument("--serve-gap-ms", type=float, default=2.0)
+    ap.add_argument("--serve-precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--serve-budget-gb", type=float, default=120.0)
+    ap.add_argument("--serve-round", type=int, default=16)
+    ap.add_argument("--serve-step-gb", type=float, default=2.0)
     args = ap.parse_args()
+    if args.serve:
+        return run_serve(args)
     if args.kernel_only:
         return run_kernel_only(args)
     if args.kubo:

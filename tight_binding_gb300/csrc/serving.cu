@@ -40,9 +40,12 @@
 namespace tbk {
 namespace {
 
+#ifndef TBK_SERVE_MIN_BLOCKS
+#define TBK_SERVE_MIN_BLOCKS 4      // resident CTAs per SM the step kernel is compiled for
+#endif
 constexpr int kSrvThreads = 256;
 constexpr int kSrvWarps = kSrvThreads / 32;
-constexpr int kSlabBytes = 32768;   // vector bytes per slab (fixes the summation order)
+constexpr int kIterPerSlab = 8;        // warp iterations (512 B of v_s each) per slab
 constexpr int kGroups = 32;         // group code = (prec * 8 + log2(width)) * 2 + complex
 
 struct SLane {                      // up to 64 vectors of one request (device view)
@@ -53,7 +56,7 @@ struct SLane {                      // up to 64 vectors of one request (device v
   void* va;                         // v_s for even s
   void* vb;                         // v_s for odd s
   int32_t n, n_steps, s0, req;
-  int32_t slab_begin, n_slabs, pad0, pad1;
+  int32_t slab_begin, n_slabs, slab_rows, pad;
 };
 struct SSlab {
   int32_t lane, row0;
@@ -71,20 +74,22 @@ struct SHdr {
 
 // complex element size cs = 8 (complex64) or 16 (complex128); width R
 __host__ __device__ constexpr int srv_vpl(int cs, int R) { return (cs == 8 && R >= 2) ? 2 : 1; }
-__host__ __device__ constexpr int srv_rows_per_tile(int cs, int R) { return (32 / (R / srv_vpl(cs, R))) * kSrvWarps; }
-__host__ __device__ constexpr int srv_slab_rows(int cs, int R) {
-  return (kSlabBytes / (R * cs)) < srv_rows_per_tile(cs, R) ? srv_rows_per_tile(cs, R) : kSlabBytes / (R * cs);
-}
+__host__ __device__ constexpr int srv_rows_per_warp(int cs, int R) { return 32 / (R / srv_vpl(cs, R)); }
+// Rows per slab: eight warp iterations, 4 KB of v_s.  The slab is the unit of
+// one moment partial, so this fixes the summation order; it depends on (cs, R)
+// alone.
+inline int srv_slab_rows(int cs, int R, int64_t) { return srv_rows_per_warp(cs, R) * kIterPerSlab; }
 
-// One doubling recursion step (step j of the round) over the slabs of group g.
-// Per slab, with s = s0 + j the lane's step: x = v_s, y = v_{s-1} on entry,
+// One doubling recursion step (step j of the round) over the slabs of group g,
+// one warp per slab (no barriers: warps run independently).  With s = s0 + j
+// the lane's step, x = v_s and y = v_{s-1} on entry:
 //   s == 0:         y = H x,             partials <x|x>, <x|y>
 //   0 < s < last:   y = 2 H x - y,       partials <x|x>, <x|y_in>
 //   s == last:      no product, no store, partials <x|x>, <x|y_in>
 // which are the step sums of the doubling identities mu_2s = 2<v_s|v_s> - mu_0,
 // mu_2s-1 = 2<v_s|v_s-1> - mu_1.
 template <typename F, int R, bool CPLX_H>
-__global__ void __launch_bounds__(kSrvThreads) srv_step_kernel(
+__global__ void __launch_bounds__(kSrvThreads, TBK_SERVE_MIN_BLOCKS) srv_step_kernel(
     const SHdr* __restrict__ hdr, const SLane* __restrict__ lanes, const SSlab* __restrict__ slabs, int32_t g,
     int32_t j, int32_t reverse, int32_t pf_dist, double* __restrict__ part, int32_t slab_cap) {
   using CT = typename C2<F>::T;
@@ -92,30 +97,49 @@ __global__ void __launch_bounds__(kSrvThreads) srv_step_kernel(
   constexpr int VPL = srv_vpl(CS, R);
   constexpr int LPR = R / VPL;
   constexpr int RPW = 32 / LPR;
-  constexpr int RPT = srv_rows_per_tile(CS, R);
-  constexpr int SLAB_ROWS = srv_slab_rows(CS, R);
   static_assert(LPR >= 1 && LPR <= 32 && (32 % LPR) == 0, "width out of range");
-  static_assert(SLAB_ROWS % RPT == 0 && SLAB_ROWS % 32 == 0, "slab must hold whole tiles and slices");
 
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31;
   const int sub = lane % LPR;
   const int32_t begin = hdr->grp_begin[g], cnt = hdr->grp_count[g];
-  __shared__ double sh[2][2][kSrvWarps];
-  int par = 0;
-  for (int32_t t = blockIdx.x; t < cnt; t += gridDim.x) {
+  const int32_t nw = (int32_t)gridDim.x * kSrvWarps;
+  int32_t t = (int32_t)blockIdx.x * kSrvWarps + (threadIdx.x >> 5);
+  SSlab nxt = t < cnt ? slabs[begin + (reverse ? cnt - 1 - t : t)] : SSlab{-1, 0};
+  // fields of the lane last seen (consecutive slabs of a warp mostly share it)
+  int32_t cl = -1, n = 0, ns = 0, s = 0, slab_rows = 0;
+  const CT* xa = nullptr;
+  CT* ya = nullptr;
+  const int32_t* soff = nullptr;
+  const int32_t* ecol = nullptr;
+  const F* eval = nullptr;
+  const F* diag = nullptr;
+  for (; t < cnt; t += nw) {
     const int32_t i = reverse ? cnt - 1 - t : t;
-    const SSlab sl = slabs[begin + i];
-    const SLane* L = lanes + sl.lane;
-    const int32_t n = L->n, ns = L->n_steps, s = L->s0 + j;
-    if (s >= ns) continue;                       // uniform over the CTA
-    if (pf_dist > 0 && threadIdx.x == 0) {
-      // the slab this CTA reaches pf_dist iterations later: its rows of v_s, v_{s-1} into L2
-      const int32_t tf = t + pf_dist * (int32_t)gridDim.x;
+    const SSlab sl = nxt;
+    if (t + nw < cnt) nxt = slabs[begin + (reverse ? cnt - 1 - (t + nw) : t + nw)];   // in flight meanwhile
+    if (sl.lane != cl) {
+      const SLane* L = lanes + sl.lane;
+      cl = sl.lane;
+      n = L->n;
+      ns = L->n_steps;
+      s = L->s0 + j;
+      slab_rows = L->slab_rows;
+      xa = static_cast<const CT*>((s & 1) ? L->vb : L->va);
+      ya = static_cast<CT*>((s & 1) ? L->va : L->vb);
+      soff = L->soff;
+      ecol = L->ecol;
+      eval = static_cast<const F*>(L->eval);
+      diag = static_cast<const F*>(L->diag);
+    }
+    if (s >= ns) continue;                       // uniform over the warp
+    if (pf_dist > 0 && lane == 0) {
+      // the slab this warp reaches pf_dist iterations later: v_s, v_{s-1} rows into L2
+      const int32_t tf = t + pf_dist * nw;
       if (tf < cnt) {
         const SSlab sf = slabs[begin + (reverse ? cnt - 1 - tf : tf)];
         const SLane* Lf = lanes + sf.lane;
         const int32_t sfs = Lf->s0 + j;
-        const int32_t nr = min(SLAB_ROWS, Lf->n - sf.row0);
+        const int32_t nr = min(Lf->slab_rows, Lf->n - sf.row0);
         if (sfs < Lf->n_steps && nr > 0) {
           const uint32_t nb = (uint32_t)nr * (uint32_t)(R * CS);
           if ((nb & 15u) == 0) {
@@ -129,16 +153,12 @@ __global__ void __launch_bounds__(kSrvThreads) srv_step_kernel(
     }
     const bool first = s == 0;
     const bool dot_only = s == ns - 1 && s > 0;
-    const CT* x = static_cast<const CT*>((s & 1) ? L->vb : L->va);
-    CT* y = static_cast<CT*>((s & 1) ? L->va : L->vb);
-    const int32_t* soff = L->soff;
-    const int32_t* ecol = L->ecol;
-    const F* eval = static_cast<const F*>(L->eval);
-    const F* diag = static_cast<const F*>(L->diag);
-    const int32_t rend = min(sl.row0 + SLAB_ROWS, n);
+    const CT* x = xa;
+    CT* y = ya;
+    const int32_t rend = min(sl.row0 + slab_rows, n);
     F m0 = 0, m1 = 0;
-    for (int32_t rb = sl.row0; rb < rend; rb += RPT) {
-      const int32_t r = rb + warp * RPW + lane / LPR;
+    for (int32_t rb = sl.row0; rb < rend; rb += RPW) {
+      const int32_t r = rb + lane / LPR;
       if (r >= rend) break;
       const int64_t me = (int64_t)r * LPR + sub;
       const LaneV<F, VPL> xs = ld_ro<F, VPL>(x + me * VPL);
@@ -188,56 +208,56 @@ __global__ void __launch_bounds__(kSrvThreads) srv_step_kernel(
       }
       if (!dot_only) st_v<F, VPL>(y + me * VPL, out);
     }
-    // slab partial in FP64: fixed warp tree, then the warps in order
+    // slab partial in FP64: a fixed shuffle tree, lane 0 writes
     double d0 = (double)m0, d1 = (double)m1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       d0 += __shfl_xor_sync(0xffffffffu, d0, o);
       d1 += __shfl_xor_sync(0xffffffffu, d1, o);
     }
-    if (lane == 0) { sh[par][0][warp] = d0; sh[par][1][warp] = d1; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double a = 0.0, b = 0.0;
-#pragma unroll
-      for (int q = 0; q < kSrvWarps; ++q) { a += sh[par][0][q]; b += sh[par][1][q]; }
+    if (lane == 0) {
       double* p = part + ((int64_t)j * slab_cap + begin + i) * 2;
-      p[0] = a;
-      p[1] = b;
+      p[0] = d0;
+      p[1] = d1;
     }
-    par ^= 1;   // the next slab writes the other half: one barrier per slab suffices
   }
 }
 
-// Step sums of every running request: one warp per (request, step of the
-// round); lane l adds slabs l, l+32, ... of each lane block in order, then a
-// fixed shuffle tree; lane 0 writes.
-__global__ void srv_reduce_kernel(const SHdr* __restrict__ hdr, const SLane* __restrict__ lanes,
-                                  const SReq* __restrict__ reqs, const double* __restrict__ part, int32_t slab_cap,
-                                  int32_t S) {
-  const int32_t lane = threadIdx.x & 31;
-  const int32_t nw = (int32_t)((gridDim.x * blockDim.x) >> 5);
+// Step sums of every running request: one CTA per (request, step of the
+// round); thread k adds slabs k, k+256, ... of each lane in order, then a fixed
+// tree in shared memory; thread 0 writes.
+constexpr int kReduceThreads = 256;
+__global__ void __launch_bounds__(kReduceThreads) srv_reduce_kernel(
+    const SHdr* __restrict__ hdr, const SLane* __restrict__ lanes, const SReq* __restrict__ reqs,
+    const double* __restrict__ part, int32_t slab_cap, int32_t S) {
+  __shared__ double sh[2][kReduceThreads];
   const int32_t total = hdr->n_reqs * S;
-  for (int32_t w = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < total; w += nw) {
+  for (int32_t w = blockIdx.x; w < total; w += gridDim.x) {
     const int32_t q = w / S, j = w - q * S;
     const SReq rq = reqs[q];
     const int32_t s = rq.s0 + j;
-    if (s >= rq.n_steps) continue;
+    if (s >= rq.n_steps) continue;               // uniform over the CTA
     double t0 = 0.0, t1 = 0.0;
     for (int32_t c = 0; c < rq.n_lanes; ++c) {
       const SLane& L = lanes[rq.lane0 + c];
       const double* p = part + ((int64_t)j * slab_cap + L.slab_begin) * 2;
       double a0 = 0.0, a1 = 0.0;
-      for (int32_t k = lane; k < L.n_slabs; k += 32) { a0 += p[2 * k]; a1 += p[2 * k + 1]; }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
-        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      for (int32_t k = threadIdx.x; k < L.n_slabs; k += kReduceThreads) { a0 += p[2 * k]; a1 += p[2 * k + 1]; }
+      sh[0][threadIdx.x] = a0;
+      sh[1][threadIdx.x] = a1;
+      __syncthreads();
+      for (int o = kReduceThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+          sh[0][threadIdx.x] += sh[0][threadIdx.x + o];
+          sh[1][threadIdx.x] += sh[1][threadIdx.x + o];
+        }
+        __syncthreads();
       }
-      t0 += a0;
-      t1 += a1;
+      t0 += sh[0][0];
+      t1 += sh[1][0];
+      __syncthreads();
     }
-    if (lane == 0) { rq.sums[2 * s] = t0; rq.sums[2 * s + 1] = t1; }
+    if (threadIdx.x == 0) { rq.sums[2 * s] = t0; rq.sums[2 * s + 1] = t1; }
   }
 }
 
@@ -448,7 +468,7 @@ struct SrvRequest {
   std::vector<DevBuf> vec;           // va, vb per lane
   DevBuf sums;
   int64_t mu_off = -1;
-  int32_t rc = 0, cs = 0, n_lanes = 0, n_steps = 0, s0 = 0, code = 0, n = 0;
+  int32_t rc = 0, cs = 0, n_lanes = 0, n_steps = 0, s0 = 0, code = 0, n = 0, slab_rows = 0;
   double step_bytes = 0.0;           // algorithmic bytes of one full step
   double mat_bytes = 0.0, vec_bytes = 0.0;
   std::vector<double> mu;
@@ -571,6 +591,7 @@ int build_request(tbk_server_s* S, SrvRequest* r) {
   r->n_lanes = (q.R + r->rc - 1) / r->rc;
   r->n_steps = steps_for(q.n_mom);
   r->code = group_code(q.precision, r->rc, q.is_complex != 0);
+  r->slab_rows = srv_slab_rows(r->cs, r->rc, r->n);
   const int64_t Np = (int64_t)Ht->ell.n_slices * 32;
   const size_t blk = (size_t)Np * r->rc * r->cs;
   r->vec.resize(2 * (size_t)r->n_lanes);
@@ -707,7 +728,7 @@ int capture_graph(tbk_server_s* S, uint32_t mask, cudaGraphExec_t* out) {
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st, S->ev_join[code], 0);
   }
   if (e == cudaSuccess && rc == TBK_OK) {
-    srv_reduce_kernel<<<S->sms * 4, 256, 0, st>>>(a.hdr, a.lanes, reinterpret_cast<const SReq*>(base + S->off_reqs),
+    srv_reduce_kernel<<<S->sms * 8, kReduceThreads, 0, st>>>(a.hdr, a.lanes, reinterpret_cast<const SReq*>(base + S->off_reqs),
                                                  a.part, a.slab_cap, S->S);
     e = cudaGetLastError();
   }
@@ -761,7 +782,7 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
   std::stable_sort(order.begin(), order.end(), [](SrvRequest* a, SrvRequest* b) { return a->code < b->code; });
   int32_t n_lanes = 0, n_slabs = 0;
   for (SrvRequest* r : order) {
-    const int32_t sr = srv_slab_rows(r->cs, r->rc);
+    const int32_t sr = r->slab_rows;
     n_lanes += r->n_lanes;
     n_slabs += r->n_lanes * ((r->n + sr - 1) / sr);
   }
@@ -785,7 +806,7 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
     SrvRequest* r = order[qi];
     const int code = r->code;
     if (!(mask & (1u << code))) { mask |= 1u << code; hdr->grp_begin[code] = si; }
-    const int32_t sr = srv_slab_rows(r->cs, r->rc);
+    const int32_t sr = r->slab_rows;
     const int32_t steps = std::min(S->S, r->n_steps - r->s0);
     SReq& q = reqs[qi];
     q.sums = r->sums.as<double>();
@@ -812,7 +833,8 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
       L.req = qi;
       L.slab_begin = si;
       L.n_slabs = (r->n + sr - 1) / sr;
-      L.pad0 = L.pad1 = 0;
+      L.slab_rows = sr;
+      L.pad = 0;
       for (int32_t k = 0; k < L.n_slabs; ++k) slabs[si + k] = SSlab{li, k * sr};
       si += L.n_slabs;
       ++li;
@@ -920,7 +942,8 @@ void loop_main(tbk_server_s* S) {
 }
 
 // Times each candidate launch shape of every real group on a synthetic width-4
-// operator of ~64 MB of vectors and keeps the fastest (grid, prefetch distance).
+// operator of ~64 MB per vector block (TBK_SERVE_TUNE_MB overrides) and keeps
+// the fastest (grid, prefetch distance).
 int autotune(tbk_server_s* S) {
   cudaStream_t st = S->st_loop;
   cudaEvent_t e0, e1;
@@ -932,8 +955,10 @@ int autotune(tbk_server_s* S) {
       const int code = group_code(prec, rc, false);
       const GroupFns fn = group_fns(code);
       const int cs = prec == TBK_PREC_MIXED ? 8 : 16;
-      const int sr = srv_slab_rows(cs, rc);
-      int32_t n = (int32_t)((64ll << 20) / ((int64_t)rc * cs));
+      int64_t tune_mb = 64;
+      if (const char* ev = getenv("TBK_SERVE_TUNE_MB")) tune_mb = std::max(1, atoi(ev));   // tuning override
+      int32_t n = (int32_t)((tune_mb << 20) / ((int64_t)rc * cs));
+      const int sr = srv_slab_rows(cs, rc, n);
       n = std::max(sr, n / sr * sr);
       const int32_t ns = n / 32, n_slab = n / sr;
       DevBuf soff, ecol, eval, diag, va, vb, tab, prt;
@@ -973,6 +998,7 @@ int autotune(tbk_server_s* S) {
       L->s0 = 1;
       L->slab_begin = 0;
       L->n_slabs = n_slab;
+      L->slab_rows = sr;
       SSlab* sl = reinterpret_cast<SSlab*>(h.data() + off_s);
       for (int32_t k = 0; k < n_slab; ++k) sl[k] = SSlab{0, k * sr};
       TBK_TRY(tab.alloc(h.size()));
@@ -1088,7 +1114,11 @@ int tbk_server_create(tbk_server* out, const tbk_server_config* cfg) {
   };
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&S->st_loop, cudaStreamNonBlocking)) != cudaSuccess) return bad(e, "stream");
-  if ((e = cudaStreamCreateWithFlags(&S->st_admit, cudaStreamNonBlocking)) != cudaSuccess) return bad(e, "stream");
+  // builds run beside saturating rounds: their short kernels take SMs first
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  if ((e = cudaStreamCreateWithPriority(&S->st_admit, cudaStreamNonBlocking, prio_hi)) != cudaSuccess)
+    return bad(e, "stream");
   for (int g = 0; g < kGroups; ++g) {
     if ((e = cudaStreamCreateWithFlags(&S->side[g], cudaStreamNonBlocking)) != cudaSuccess) return bad(e, "stream");
     if ((e = cudaEventCreateWithFlags(&S->ev_join[g], cudaEventDisableTiming)) != cudaSuccess) return bad(e, "event");

@@ -21,6 +21,31 @@ from . import capi
 from .capi import check, lib
 from .lattice import PartialLattice
 
+# lattices of the serving workload: nearest-neighbour hopping from every atom
+# (TB/models.h:5-151 cells), coordination number for the spectral bounds
+MODEL_ATOMS = {"square": ("A",), "honeycomb": ("A", "B"), "kagome": ("A", "B", "C"), "lieb": ("A", "B", "C"),
+               "fcc": ("A",)}
+MODEL_COORD = {"square": 4, "honeycomb": 3, "kagome": 4, "lieb": 4, "fcc": 12}
+
+
+def model_cell(kind: str, t: float = 1.0):
+    """Unit cell of `kind` with nearest-neighbour hopping t from every atom (the
+    h.c. duplicates that later atoms would add are skipped, as the reference's
+    add_hopping does)."""
+    from . import lattice as lat
+    c = {"square": lat.Square, "honeycomb": lat.Honeycomb, "kagome": lat.Kagome, "lieb": lat.Lieb,
+         "fcc": lat.FCC}[kind]()
+    for a in MODEL_ATOMS[kind]:
+        c.add_hopping(a, 1, t)
+    return c
+
+
+def model_bounds(kind: str, W: float, t: float = 1.0, margin: float = 0.05) -> tuple[float, float]:
+    """Symmetric spectral bounds z|t| + W/2 + margin for on-site disorder U[-W/2, W/2]."""
+    e = MODEL_COORD[kind] * abs(t) + W / 2 + margin
+    return -e, e
+
+
 PRECISION = {"mixed": capi.PREC_MIXED, "fp64": capi.PREC_FP64}
 MODES = {"periodic": capi.BUILD_PERIODIC_BARE, "open": capi.BUILD_SPARSE, "bare": capi.BUILD_BARE}
 STATS_KEYS = ("done", "failed", "rounds", "graphs", "busy_ms", "bytes", "updates", "launches", "budget_bytes",
