@@ -522,6 +522,29 @@ def run_serve(args):
     return 0
 
 
+def run_serve_single(args):
+    """Profiling case of the serving step kernel: one honeycomb --cells^2 request
+    (t = 1, disorder W = 1 seed 1, R = 32, M = --moments, mixed) through a server
+    with the launch-shape tuner off, twice; reports the second's HBM rate."""
+    import tight_binding_gb300 as tb
+    from tight_binding_gb300.serving import model_bounds, model_cell
+
+    srv = tb.DosServer(autotune=False)
+    X = tb.PartialLattice(model_cell("honeycomb"), (args.cells, args.cells))
+    X.set_scalar_disorder(1.0, 1)
+    lo, hi = model_bounds("honeycomb", 1.0)
+    for _ in range(2):
+        b0 = srv.stats()
+        mu, t = srv.result(srv.submit(X, args.moments, R_VEC, seed=0, e_min=lo, e_max=hi))
+        b1 = srv.stats()
+    gbs = (b1["bytes"] - b0["bytes"]) / ((b1["busy_ms"] - b0["busy_ms"]) / 1e3) / 1e9
+    print(json.dumps({"serve_single": f"honeycomb {args.cells}^2", "sites": X.get_total_number(),
+                      "moments": args.moments, "GBps": gbs, "rounds": b1["rounds"] - b0["rounds"],
+                      "busy_ms": b1["busy_ms"] - b0["busy_ms"], "mu0": float(mu[0])}), flush=True)
+    srv.close()
+    return 0
+
+
 def run_kernel_only(args):
     """Small case of the same kernel for ncu captures: one mixed-precision DoS
     solve (doubling) on a honeycomb of --cells^2 cells, R = 32."""
@@ -571,7 +594,11 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=120.0)
     ap.add_argument("--serve-round", type=int, default=16)
     ap.add_argument("--serve-step-gb", type=float, default=2.0)
+    ap.add_argument("--serve-single", action="store_true",
+                    help="one honeycomb --cells^2 request through the server (profiling case)")
     args = ap.parse_args()
+    if args.serve_single:
+        return run_serve_single(args)
     if args.serve:
         return run_serve(args)
     if args.kernel_only:

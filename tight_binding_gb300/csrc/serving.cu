@@ -512,7 +512,7 @@ struct tbk_server_s {
   char* stage[2] = {nullptr, nullptr};
   cudaEvent_t copy_ev[2] = {nullptr, nullptr};
   bool copy_pending[2] = {false, false};
-  std::unordered_map<uint32_t, cudaGraphExec_t> graphs;
+  std::unordered_map<uint64_t, cudaGraphExec_t> graphs;   // key: group mask | round length << 32
   // launch shapes per group code
   int grid[kGroups] = {};
   int pf[kGroups] = {};
@@ -696,8 +696,9 @@ int ensure_tables(tbk_server_s* S, int32_t lanes, int32_t slabs, int32_t reqs) {
   return TBK_OK;
 }
 
-int capture_graph(tbk_server_s* S, uint32_t mask, cudaGraphExec_t* out) {
-  auto it = S->graphs.find(mask);
+int capture_graph(tbk_server_s* S, uint32_t mask, int steps, cudaGraphExec_t* out) {
+  const uint64_t key = (uint64_t)mask | ((uint64_t)steps << 32);
+  auto it = S->graphs.find(key);
   if (it != S->graphs.end()) { *out = it->second; return TBK_OK; }
   cudaStream_t st = S->st_loop;
   const char* base = S->dtab.as<char>();
@@ -719,7 +720,7 @@ int capture_graph(tbk_server_s* S, uint32_t mask, cudaGraphExec_t* out) {
     a.code = code;
     a.grid = S->grid[code];
     a.pf = S->pf[code];
-    for (int j = 0; j < S->S && e == cudaSuccess && rc == TBK_OK; ++j) {
+    for (int j = 0; j < steps && e == cudaSuccess && rc == TBK_OK; ++j) {
       a.j = j;
       a.reverse = j & 1;
       rc = fn.launch(a, sd);
@@ -729,7 +730,7 @@ int capture_graph(tbk_server_s* S, uint32_t mask, cudaGraphExec_t* out) {
   }
   if (e == cudaSuccess && rc == TBK_OK) {
     srv_reduce_kernel<<<S->sms * 8, kReduceThreads, 0, st>>>(a.hdr, a.lanes, reinterpret_cast<const SReq*>(base + S->off_reqs),
-                                                 a.part, a.slab_cap, S->S);
+                                                 a.part, a.slab_cap, steps);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && rc == TBK_OK) {
@@ -747,7 +748,7 @@ int capture_graph(tbk_server_s* S, uint32_t mask, cudaGraphExec_t* out) {
   e = cudaGraphInstantiate(&x, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(TBK_ERR_CUDA, "round instantiate: %s", cudaGetErrorString(e));
-  S->graphs[mask] = x;
+  S->graphs[key] = x;
   ++S->n_graphs;
   *out = x;
   return TBK_OK;
@@ -780,6 +781,13 @@ int reap(tbk_server_s* S, Round& rd) {
 int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Round>& inflight, int64_t round_id) {
   std::vector<SrvRequest*> order(run);
   std::stable_sort(order.begin(), order.end(), [](SrvRequest* a, SrvRequest* b) { return a->code < b->code; });
+  // round length: S, or the next power of two covering the longest remainder
+  // (so that a lone short tail does not run empty launches)
+  int32_t left = 0;
+  for (SrvRequest* r : run) left = std::max(left, r->n_steps - r->s0);
+  int32_t RS = 1;
+  while (RS < left && RS < S->S) RS <<= 1;
+  RS = std::min(RS, S->S);
   int32_t n_lanes = 0, n_slabs = 0;
   for (SrvRequest* r : order) {
     const int32_t sr = r->slab_rows;
@@ -807,7 +815,7 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
     const int code = r->code;
     if (!(mask & (1u << code))) { mask |= 1u << code; hdr->grp_begin[code] = si; }
     const int32_t sr = r->slab_rows;
-    const int32_t steps = std::min(S->S, r->n_steps - r->s0);
+    const int32_t steps = std::min(RS, r->n_steps - r->s0);
     SReq& q = reqs[qi];
     q.sums = r->sums.as<double>();
     q.mu = S->arena_host + r->mu_off;
@@ -816,7 +824,7 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
     q.s0 = r->s0;
     q.n_steps = r->n_steps;
     q.n_mom = r->q.n_mom;
-    q.finishing = r->s0 + S->S >= r->n_steps ? 1 : 0;
+    q.finishing = r->s0 + RS >= r->n_steps ? 1 : 0;
     const EllDev& E = r->Ht->ell;
     const bool mixed = r->q.precision == TBK_PREC_MIXED;
     for (int32_t c = 0; c < r->n_lanes; ++c) {
@@ -853,7 +861,7 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
   hdr->n_slabs = si;
   hdr->n_reqs = n_reqs;
   cudaGraphExec_t gx = nullptr;
-  TBK_TRY(capture_graph(S, mask, &gx));
+  TBK_TRY(capture_graph(S, mask, RS, &gx));
   cudaStream_t st = S->st_loop;
   char* db = S->dtab.as<char>();
   TBK_CUDA(cudaMemcpyAsync(db, hb, sizeof(SHdr), cudaMemcpyHostToDevice, st));
@@ -869,11 +877,11 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
   TBK_CUDA(cudaEventRecord(rd.ev1, st));
   int groups = 0;
   for (int c = 0; c < kGroups; ++c) groups += (mask >> c) & 1;
-  rd.launches = (int64_t)groups * S->S + 2;
+  rd.launches = (int64_t)groups * RS + 2;
   // advance: who is left for the next round
   std::vector<SrvRequest*> next;
   for (SrvRequest* r : run) {
-    r->s0 += S->S;
+    r->s0 += RS;
     if (r->s0 < r->n_steps) next.push_back(r);
   }
   run.swap(next);
