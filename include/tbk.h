@@ -218,13 +218,19 @@ int tbk_dos_from_moments(int32_t n, const double* mu, int32_t kernel_kind, doubl
 /* =========================================================================
  * Kubo conductivities from double-Chebyshev moments.
  * ========================================================================= */
-enum { TBK_MU_CUDA_CORE = 0, TBK_MU_TENSOR = 1 };
+enum {
+  TBK_MU_CUDA_CORE = 0,             /* mu_nm GEMM on CUDA cores (FP32 chunks, FP64 sums) */
+  TBK_MU_TENSOR = 1,                /* mu_nm GEMM on tcgen05 (split TF32)               */
+  TBK_MU_MIXED_RECURSION = 2        /* complex64 recursion for the stored blocks (FP32
+                                       H~); default: complex128 recursion, FP64 H~      */
+};
 /* mu_mn = sum_{sites,r} conj(aL_m) aR_n with aL_m = g_m AL T_m(H~) BL |r>,
  * aR_n = g_n AR T_n(H~) BR |r> (NULL operator = identity), m, n < M: the stored
  * Chebyshev blocks of TB/numerical.h:333-344 contracted as in TB/snippets.h:
  * 337-342 (Bastin: AL=BL=1, AR=v_x, BR=v_y), :225-260 (Greenwood: AL=BL=v_x)
  * and :491-518 (generate_V_moments).  Blocks are complex64 in HBM; R vectors
- * are processed in chunks so both sides fit block_budget_gb (<= 0: 40 GB).
+ * are processed in chunks so both sides fit block_budget_gb (<= 0: 60% of the
+ * free device memory).
  * kets: host N x R column-major complex128, or NULL for seeded random phases.
  * kernel: TBK_KERNEL_* with parameters kp0/kp1 (g_m).  flags: TBK_MU_*.
  * mu_out: host M x M complex128, row m = left index. */

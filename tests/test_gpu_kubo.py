@@ -128,3 +128,45 @@ def test_greenwood_spectrum_and_v_moments(gpu):
     kets = orc.random_phase_kets(40, 6, 0)
     ref = np.triu(np.real(orc.kubo_mu(40, cp, ri, v, 12, kets, AL=vel, BL=vel)) / 6)
     assert _rel(V, ref) <= MU_TOL
+
+
+@pytest.mark.parametrize("which", ["bastin", "greenwood"])
+def test_mu_nm_mixed_recursion(gpu, which):
+    """complex64 recursion (FP32 H~) for the stored blocks: same bound as the
+    complex128 recursion on M = 32."""
+    tb = gpu
+    X, H = _system(tb)
+    G = tb.GreenFunction(32, H, -4.1, 4.1)
+    Ht = G.scaled_HE
+    v_x = tb.commutator(Ht, X.op_position(0))
+    v_y = tb.commutator(Ht, X.op_position(1))
+    n, cp, ri, v, ovx, ovy = _oracle_ops(tb, X, Ht)
+    kets = orc.random_phase_kets(n, 3, 2)
+    g = orc.kernel_seq(orc.K_LORENTZ, 32, 6.0)
+    if which == "bastin":
+        mu = tb.kubo_mu(Ht, None, None, v_x, v_y, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True,
+                        recursion="mixed")
+        ref = orc.kubo_mu(n, cp, ri, v, 32, kets, AR=ovx, BR=ovy, g=g)
+    else:
+        mu = tb.kubo_mu(Ht, v_x, v_x, None, None, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True,
+                        recursion="mixed")
+        ref = orc.kubo_mu(n, cp, ri, v, 32, kets, AL=ovx, BL=ovx, g=g)
+    assert _rel(mu, ref) <= MU_TOL, _rel(mu, ref)
+
+
+def test_bastin_sigma_xy_mixed_recursion(gpu):
+    """sigma_xy with the complex64 recursion: stated bound 1e-5 of max |sigma| of
+    the FP64 oracle pipeline (as the complex128 recursion), M = 64."""
+    tb = gpu
+    X, H = _system(tb, (16, 16), flux=1 / 16)
+    N, R = 64, 4
+    out = tb.conductivity_Kubo_Bastin(H, X.op_position(0), X.op_position(1), N, -4.0, 4.0, R=R, seed=2,
+                                      tensor=True, recursion="mixed")
+    Ht = out["G"].scaled_HE
+    n, cp, ri, v, ovx, ovy = _oracle_ops(tb, X, Ht)
+    kets = orc.random_phase_kets(n, R, 2)
+    g = orc.kernel_seq(orc.K_LORENTZ, N, 6.0)
+    mu = orc.kubo_mu(n, cp, ri, v, N, kets, AR=ovx, BR=ovy, g=g)
+    eps = tb.chebyshev_nodes(N)
+    E, sr, si = orc.bastin_integrate(eps, orc.bastin_zeta(mu, eps, 1.0))
+    assert _rel(out["sigma_re"], sr) <= 1e-5, _rel(out["sigma_re"], sr)

@@ -34,7 +34,7 @@ BUILD_SPARSE = 0
 BUILD_PERIODIC_BARE = 1
 BUILD_BARE = 2
 
-MU_CUDA_CORE, MU_TENSOR = 0, 1
+MU_CUDA_CORE, MU_TENSOR, MU_MIXED_RECURSION = 0, 1, 2
 
 KERNEL_DIRICHLET, KERNEL_FEJER, KERNEL_LORENTZ, KERNEL_JACKSON, KERNEL_LANCZOS, KERNEL_WANG_ZUNGER = range(6)
 

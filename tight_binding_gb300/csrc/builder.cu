@@ -433,7 +433,7 @@ __global__ void slice_width_kernel(int32_t n, int32_t n_slices, const int32_t* _
 }
 
 __global__ void ell_fill_kernel(int32_t n, const int32_t* __restrict__ rp, const int32_t* __restrict__ rc,
-                                const int64_t* __restrict__ src, const double* __restrict__ v, int cplx,
+                                const int64_t* __restrict__ src, const double* __restrict__ v, int in_cplx, int cplx,
                                 const int32_t* __restrict__ soff, int32_t* __restrict__ ecol,
                                 double* __restrict__ e64, float* __restrict__ e32,
                                 double* __restrict__ d64, float* __restrict__ d32) {
@@ -446,8 +446,8 @@ __global__ void ell_fill_kernel(int32_t n, const int32_t* __restrict__ rp, const
   double dr = 0.0, di = 0.0;
   for (int32_t p = rp[i]; p < rp[i + 1]; ++p) {
     int64_t q = src[p];
-    double vr = cplx ? v[2 * q] : v[q];
-    double vi = cplx ? v[2 * q + 1] : 0.0;
+    double vr = in_cplx ? v[2 * q] : v[q];
+    double vi = in_cplx ? v[2 * q + 1] : 0.0;
     if (rc[p] == i) { dr += vr; di += vi; continue; }   // a CSC holds at most one diagonal entry per column
     int64_t o = base + (int64_t)k * 32 + l;
     ecol[o] = rc[p];
@@ -463,6 +463,12 @@ __global__ void ell_fill_kernel(int32_t n, const int32_t* __restrict__ rp, const
   }
   if (cplx) { d64[2 * i] = dr; d64[2 * i + 1] = di; d32[2 * i] = __double2float_rn(dr); d32[2 * i + 1] = __double2float_rn(di); }
   else { d64[i] = dr; d32[i] = __double2float_rn(dr); }
+}
+
+// flag = 1 when any imaginary part of a complex value array is nonzero (or NaN)
+__global__ void imag_nonzero_kernel(int64_t nnz, const double* __restrict__ v, int* __restrict__ flag) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += (int64_t)gridDim.x * blockDim.x)
+    if (!(v[2 * q + 1] == 0.0)) { atomicOr(flag, 1); return; }
 }
 
 // Rows of the slice tail beyond n (n not a multiple of 32) still need valid
@@ -488,8 +494,25 @@ int ensure_ell(tbk_sparse_s* A, cudaStream_t st) {
   if (A->ell_ready) return TBK_OK;
   if (A->rows != A->cols) return fail(TBK_ERR_INVALID, "recursion needs a square matrix (%d x %d)", A->rows, A->cols);
   const int32_t n = A->rows;
-  const int cplx = A->is_complex;
+  const int in_cplx = A->is_complex;
+  // a complex matrix whose imaginary parts are all zero gets a real ELL: the
+  // products are the same (only the sign of an exact zero can differ) and the
+  // recursion streams half the matrix bytes
+  int cplx = in_cplx;
+  if (in_cplx && A->nnz > 0) {
+    DevBuf flag;
+    TBK_TRY(flag.alloc(sizeof(int)));
+    TBK_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), st));
+    const int64_t blocks = std::min<int64_t>((A->nnz + 255) / 256, 65535);
+    imag_nonzero_kernel<<<(unsigned)blocks, 256, 0, st>>>(A->nnz, A->values.as<double>(), flag.as<int>());
+    TBK_CHECK_LAUNCH();
+    int h = 1;
+    TBK_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TBK_CUDA(cudaStreamSynchronize(st));
+    cplx = h ? 1 : 0;
+  }
   EllDev& E = A->ell;
+  E.cplx = cplx;
   E.n_rows = n;
   E.n_slices = (n + 31) / 32;
   DevBuf cnt, rp, cur, rc, src, w32;
@@ -531,7 +554,7 @@ int ensure_ell(tbk_sparse_s* A, cudaStream_t st) {
   TBK_CUDA(cudaMemsetAsync(E.diag64.p, 0, E.diag64.bytes, st));
   TBK_CUDA(cudaMemsetAsync(E.diag32.p, 0, E.diag32.bytes, st));
   ell_fill_kernel<<<(n + T - 1) / T, T, 0, st>>>(n, rp.as<int32_t>(), rc.as<int32_t>(), src.as<int64_t>(),
-                                                  A->values.as<double>(), cplx, E.slice_off.as<int32_t>(),
+                                                  A->values.as<double>(), in_cplx, cplx, E.slice_off.as<int32_t>(),
                                                   E.col.as<int32_t>(), E.val64.as<double>(), E.val32.as<float>(),
                                                   E.diag64.as<double>(), E.diag32.as<float>());
   TBK_CHECK_LAUNCH();

@@ -378,7 +378,7 @@ int step_config(tbk_sparse_s* A, int Rc, bool fp64, int* grid, int* n_tiles, cud
   const int rpt = rows_per_tile(fp64 ? TBK_PREC_FP64 : TBK_PREC_MIXED, Rc);
   *n_tiles = (A->rows + rpt - 1) / rpt;
   int occ = 1;
-  const bool cplx = A->is_complex != 0;
+  const bool cplx = A->ell.cplx != 0;
 #define OCC2(F)                                                                                          \
   switch (Rc) {                                                                                          \
     case 1: occ = cplx ? occupancy_blocks<F, true, 1>() : occupancy_blocks<F, false, 1>(); break;        \
@@ -415,9 +415,9 @@ int step_any(tbk_sparse_s* A, int Rc, bool fp64, const void* x, void* y, const v
   a.gather = 1;
   a.pf_dist = 1;
   if (fp64)
-    return A->is_complex ? launch_step<double, true>(Rc, a, first, false, grid, st)
+    return A->ell.cplx ? launch_step<double, true>(Rc, a, first, false, grid, st)
                          : launch_step<double, false>(Rc, a, first, false, grid, st);
-  return A->is_complex ? launch_step<float, true>(Rc, a, first, false, grid, st)
+  return A->ell.cplx ? launch_step<float, true>(Rc, a, first, false, grid, st)
                        : launch_step<float, false>(Rc, a, first, false, grid, st);
 }
 
@@ -496,7 +496,7 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
   const TmaLayout& lay = braket ? P->lay_brk : P->lay_dbl;
   TBK_CUDA(cudaMemsetAsync(P->err.p, 0, sizeof(int), st));
   const bool mixed = P->prec == TBK_PREC_MIXED;
-  const bool cplx = P->H->is_complex != 0;
+  const bool cplx = P->H->ell.cplx != 0;
   float ms_total = 0.f;
   int32_t launches = 0;
   for (int32_t ch = 0; ch < P->n_chunks; ++ch) {
@@ -605,7 +605,7 @@ int tbk_kpm_create(tbk_kpm* out, tbk_sparse Ht, int32_t R, int32_t flags) {
   const int rpt = rows_per_tile(prec, rc);
   P->n_tiles = (int)((P->n + rpt - 1) / rpt);
   int occ = 1;
-  const bool cplx = Ht->is_complex != 0;
+  const bool cplx = Ht->ell.cplx != 0;
 #define OCC(F, C)                                                                 \
   switch (rc) {                                                                   \
     case 1: occ = occupancy_blocks<F, C, 1>(); break;                             \

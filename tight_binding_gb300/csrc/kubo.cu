@@ -99,12 +99,16 @@ __global__ void mu_split_reduce_kernel(const double2* __restrict__ part, int32_t
   acc[q].y += i;
 }
 
-// complex128 work block -> block m of the complex64 K-tiled store (one rounding
-// per element); 16 consecutive k form one contiguous 128-byte row of the tile
-__global__ void round_block_kernel(const double2* __restrict__ src, float2* __restrict__ store, int32_t m, int32_t M,
+// work block -> block m of the complex64 K-tiled store (complex128 work blocks
+// are rounded once per element); 16 consecutive k form one contiguous 128-byte
+// row of the tile
+__device__ __forceinline__ float2 to_c64(double2 v) { return make_float2(__double2float_rn(v.x), __double2float_rn(v.y)); }
+__device__ __forceinline__ float2 to_c64(float2 v) { return v; }
+template <typename CT>
+__global__ void round_block_kernel(const CT* __restrict__ src, float2* __restrict__ store, int32_t m, int32_t M,
                                    int64_t n) {
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
-    store[((q >> 4) * M + m) * 16 + (q & 15)] = make_float2(__double2float_rn(src[q].x), __double2float_rn(src[q].y));
+    store[((q >> 4) * M + m) * 16 + (q & 15)] = to_c64(src[q]);
 }
 
 __global__ void mu_kernel_scale_kernel(double2* __restrict__ mu, const double* __restrict__ g, int32_t M) {
@@ -228,21 +232,31 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   const int64_t n_pad = (int64_t)Ht->ell.n_slices * 32;
   // chunk of random vectors: both stored sides within the budget
   int Rc = pick_chunk(R);
-  const double budget = (block_budget_gb > 0 ? block_budget_gb : 40.0) * 1e9;
+  // default budget: 60% of the free device memory (more vectors per chunk stream
+  // the matrix fewer times)
+  double budget = block_budget_gb * 1e9;
+  if (block_budget_gb <= 0) {
+    size_t fr = 0, tot = 0;
+    TBK_CUDA(cudaMemGetInfo(&fr, &tot));
+    budget = 0.6 * (double)fr;
+  }
   while (Rc > 1 && 2.0 * M * n_pad * Rc * 8.0 > budget) Rc >>= 1;
   if (2.0 * M * n_pad * Rc * 8.0 > budget)
     return fail(TBK_ERR_BUDGET, "stored Chebyshev blocks need %.1f GB > budget %.1f GB", 2.0 * M * n_pad * 8.0 / 1e9,
                 budget / 1e9);
   const int64_t blk = n_pad * Rc;                       // complex entries per block
-  // stored blocks: complex64; recursion and operator applications: complex128
-  // work blocks (the Chebyshev recursion accumulates rounding error near the band
-  // edges, where the Kubo weights 1/(1-e^2)^2 are largest; each stored value is
-  // rounded to complex64 exactly once)
+  // stored blocks: complex64.  Recursion and operator applications: complex128
+  // work blocks by default (the Chebyshev recursion accumulates rounding error
+  // near the band edges, where the Kubo weights 1/(1-e^2)^2 are largest; each
+  // stored value is rounded to complex64 exactly once); TBK_MU_MIXED_RECURSION
+  // runs them in complex64 with FP32 H~ (HBM-bound instead of FP64-pipe-bound).
+  const bool fp64 = (flags & TBK_MU_MIXED_RECURSION) == 0;
+  const size_t csz = fp64 ? sizeof(double2) : sizeof(float2);
   DevBuf Ls, Rs, work, partd, part, macc, gdev, kstage;
   const int64_t blk16 = (blk + 15) / 16 * 16;           // K padded to whole 16-element tiles (zeros)
   TBK_TRY(Ls.alloc(sizeof(float2) * blk16 * M));
   TBK_TRY(Rs.alloc(sizeof(float2) * blk16 * M));
-  TBK_TRY(work.alloc(sizeof(double2) * blk * 6));
+  TBK_TRY(work.alloc(csz * blk * 6));
   TBK_CUDA(cudaMemsetAsync(Ls.p, 0, Ls.bytes, st));
   TBK_CUDA(cudaMemsetAsync(Rs.p, 0, Rs.bytes, st));
   TBK_CUDA(cudaMemsetAsync(work.p, 0, work.bytes, st));
@@ -253,42 +267,45 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     TBK_CUDA(cudaMemcpyAsync(kstage.p, kets, sizeof(double2) * (size_t)n * R, cudaMemcpyHostToDevice, st));
   }
   int grid = 1, n_tiles = 1;
-  TBK_TRY(step_config(Ht, Rc, true, &grid, &n_tiles, st));
+  TBK_TRY(step_config(Ht, Rc, fp64, &grid, &n_tiles, st));
   int gmax = grid;
   for (auto* o : ops)
-    if (o) { int g2, t2; TBK_TRY(step_config(o, Rc, true, &g2, &t2, st)); gmax = std::max(gmax, g2); }
+    if (o) { int g2, t2; TBK_TRY(step_config(o, Rc, fp64, &g2, &t2, st)); gmax = std::max(gmax, g2); }
   TBK_TRY(partd.alloc(sizeof(double) * 2 * gmax));
-  double2* wb = work.as<double2>();
-  double2* v0 = wb + 5 * blk;
-  auto apply = [&](tbk_sparse_s* A, const double2* x, double2* y) -> int {   // y = A x (FP64)
+  char* wb = work.as<char>();
+  auto wblk = [&](int i) { return static_cast<void*>(wb + (size_t)i * blk * csz); };
+  void* v0 = wblk(5);
+  auto apply = [&](tbk_sparse_s* A, const void* x, void* y) -> int {   // y = A x
     int g, t;
-    TBK_TRY(step_config(A, Rc, true, &g, &t, st));
-    return step_any(A, Rc, true, x, y, nullptr, true, partd.as<double>(), g, t, st);
+    TBK_TRY(step_config(A, Rc, fp64, &g, &t, st));
+    return step_any(A, Rc, fp64, x, y, nullptr, true, partd.as<double>(), g, t, st);
   };
-  auto round_to = [&](const double2* src, float2* store, int32_t m) -> int {
-    round_block_kernel<<<(unsigned)std::min<int64_t>((blk + 255) / 256, 65535), 256, 0, st>>>(src, store, m, M, blk);
+  auto round_to = [&](const void* src, float2* store, int32_t m) -> int {
+    const unsigned g = (unsigned)std::min<int64_t>((blk + 255) / 256, 65535);
+    if (fp64) round_block_kernel<double2><<<g, 256, 0, st>>>(static_cast<const double2*>(src), store, m, M, blk);
+    else round_block_kernel<float2><<<g, 256, 0, st>>>(static_cast<const float2*>(src), store, m, M, blk);
     TBK_CHECK_LAUNCH();
     return TBK_OK;
   };
   // one side: store[m] = Aout T_m(H~) (Bin v0), m < M
   auto side = [&](tbk_sparse_s* Aout, tbk_sparse_s* Bin, float2* store) -> int {
-    double2* r[3] = {wb, wb + blk, wb + 2 * blk};
-    double2* tmpA = wb + 3 * blk;
+    void* r[3] = {wblk(0), wblk(1), wblk(2)};
+    void* tmpA = wblk(3);
     if (Bin) TBK_TRY(apply(Bin, v0, r[0]));
-    else TBK_CUDA(cudaMemcpyAsync(r[0], v0, sizeof(double2) * blk, cudaMemcpyDeviceToDevice, st));
+    else TBK_CUDA(cudaMemcpyAsync(r[0], v0, csz * blk, cudaMemcpyDeviceToDevice, st));
     for (int32_t m = 0; m < M; ++m) {
-      double2* y = r[m % 3];
+      void* y = r[m % 3];
       if (m >= 1) {
-        const double2* x = r[(m - 1) % 3];
-        const double2* pv = m >= 2 ? r[(m - 2) % 3] : nullptr;
-        TBK_TRY(step_any(Ht, Rc, true, x, y, pv, m == 1, partd.as<double>(), grid, n_tiles, st));
+        const void* x = r[(m - 1) % 3];
+        const void* pv = m >= 2 ? r[(m - 2) % 3] : nullptr;
+        TBK_TRY(step_any(Ht, Rc, fp64, x, y, pv, m == 1, partd.as<double>(), grid, n_tiles, st));
       }
       if (Aout) { TBK_TRY(apply(Aout, y, tmpA)); TBK_TRY(round_to(tmpA, store, m)); }
       else TBK_TRY(round_to(y, store, m));
     }
     return TBK_OK;
   };
-  const bool use_tc = (flags & 1) != 0;
+  const bool use_tc = (flags & TBK_MU_TENSOR) != 0;
   const int64_t ksplit = 16384;
   const int32_t nsplit = (int32_t)((blk + ksplit - 1) / ksplit);
   if (!use_tc) TBK_TRY(part.alloc(sizeof(double2) * (size_t)nsplit * M * M));
@@ -297,8 +314,8 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   KuboTiming tm;
   for (int32_t r0 = 0; r0 < R; r0 += Rc) {
     TBK_CUDA(cudaEventRecord(ev[0], st));
-    if (kets) TBK_TRY(load_block_any(true, n, R, r0, Rc, kstage.as<double2>(), v0, st));
-    else TBK_TRY(random_block_any(true, n, R, r0, Rc, seed, v0, st));
+    if (kets) TBK_TRY(load_block_any(fp64, n, R, r0, Rc, kstage.as<double2>(), v0, st));
+    else TBK_TRY(random_block_any(fp64, n, R, r0, Rc, seed, v0, st));
     TBK_TRY(side(AL, BL, Ls.as<float2>()));
     TBK_TRY(side(AR, BR, Rs.as<float2>()));
     TBK_CUDA(cudaEventRecord(ev[1], st));
@@ -355,7 +372,7 @@ int tbk_mu_from_blocks(int32_t M, int64_t K, const double* L, const double* Rb, 
     const double* src = side ? Rb : L;
     for (int32_t m = 0; m < M; ++m) {
       TBK_CUDA(cudaMemcpyAsync(stage.p, src + 2 * (int64_t)m * K, sizeof(double2) * K, cudaMemcpyHostToDevice, st));
-      round_block_kernel<<<(unsigned)std::min<int64_t>((K + 255) / 256, 4096), 256, 0, st>>>(stage.as<double2>(), dst, m,
+      round_block_kernel<double2><<<(unsigned)std::min<int64_t>((K + 255) / 256, 4096), 256, 0, st>>>(stage.as<double2>(), dst, m,
                                                                                           M, K);
       TBK_CHECK_LAUNCH();
     }

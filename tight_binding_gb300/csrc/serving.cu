@@ -590,7 +590,7 @@ int build_request(tbk_server_s* S, SrvRequest* r) {
   r->cs = mixed ? 8 : 16;
   r->n_lanes = (q.R + r->rc - 1) / r->rc;
   r->n_steps = steps_for(q.n_mom);
-  r->code = group_code(q.precision, r->rc, q.is_complex != 0);
+  r->code = group_code(q.precision, r->rc, Ht->ell.cplx != 0);
   r->slab_rows = srv_slab_rows(r->cs, r->rc, r->n);
   const int64_t Np = (int64_t)Ht->ell.n_slices * 32;
   const size_t blk = (size_t)Np * r->rc * r->cs;
@@ -611,7 +611,7 @@ int build_request(tbk_server_s* S, SrvRequest* r) {
   int64_t held = (int64_t)(E.slice_off.bytes + E.col.bytes + E.val32.bytes + E.val64.bytes + E.diag32.bytes +
                            E.diag64.bytes + r->sums.bytes);
   for (auto& v : r->vec) held += (int64_t)v.bytes;
-  const double hv = (mixed ? 4.0 : 8.0) * (q.is_complex ? 2.0 : 1.0);
+  const double hv = (mixed ? 4.0 : 8.0) * (E.cplx ? 2.0 : 1.0);
   r->mat_bytes = (double)E.n_entries * (4.0 + hv) + (double)E.n_rows * hv + 4.0 * (E.n_slices + 1);
   r->vec_bytes = (double)r->n * r->rc * r->cs;
   r->step_bytes = r->n_lanes * (3.0 * r->vec_bytes + r->mat_bytes);

@@ -90,6 +90,7 @@ struct EllDev {
   int32_t n_rows = 0, n_slices = 0;
   int64_t n_entries = 0;
   int32_t max_width = 0;
+  int32_t cplx = 0;   // value type of the ELL: complex, or real when every imaginary part is zero
   DevBuf slice_off;   // int32 [n_slices + 1]
   DevBuf col;         // int32 [n_entries]
   DevBuf val64;       // double / double2 [n_entries]
