@@ -545,6 +545,27 @@ def run_serve_single(args):
     return 0
 
 
+def run_gemm(args):
+    """mu_nm GEMM alone on seeded random complex blocks (M x K each, rounded to
+    complex64 on the device): the profiling case of the tensor-core kernel."""
+    import tight_binding_gb300 as tb
+
+    M, K = args.gemm
+    rng = np.random.default_rng(M + K)
+    L = (rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))) / np.sqrt(K)
+    R = (rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))) / np.sqrt(K)
+    tensor = not args.cuda_core_mu
+    for _ in range(2):
+        tb.mu_from_blocks(L, R, tensor=tensor)
+    t = tb.kubo_last_timing()
+    peak, src = peaks_tensor()
+    issued = t["gemm_flops"] / (t["ms_gemm"] / 1e3) / 1e12
+    print(json.dumps({"gemm": [M, K], "path": "tcgen05 3xTF32" if tensor else "CUDA-core FP32", "ms": t["ms_gemm"],
+                      "tflops_issued": issued, "tensor_util": issued / peak if tensor else None,
+                      "peak_source": src}), flush=True)
+    return 0
+
+
 def run_kernel_only(args):
     """Small case of the same kernel for ncu captures: one mixed-precision DoS
     solve (doubling) on a honeycomb of --cells^2 cells, R = 32."""
@@ -598,7 +619,11 @@ def main():
     ap.add_argument("--serve-step-gb", type=float, default=2.0)
     ap.add_argument("--serve-single", action="store_true",
                     help="one honeycomb --cells^2 request through the server (profiling case)")
+    ap.add_argument("--gemm", type=int, nargs=2, metavar=("M", "K"),
+                    help="mu_nm GEMM alone on random M x K complex blocks (profiling case)")
     args = ap.parse_args()
+    if args.gemm:
+        return run_gemm(args)
     if args.serve_single:
         return run_serve_single(args)
     if args.serve:

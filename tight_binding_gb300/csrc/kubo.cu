@@ -377,6 +377,9 @@ int tbk_mu_from_blocks(int32_t M, int64_t K, const double* L, const double* Rb, 
       TBK_CHECK_LAUNCH();
     }
   }
+  cudaEvent_t ev[2];
+  for (auto& e : ev) TBK_CUDA(cudaEventCreate(&e));
+  TBK_CUDA(cudaEventRecord(ev[0], st));
   if (flags & TBK_MU_TENSOR) {
     TBK_TRY(mu_gemm_tc(Ld.as<float2>(), Rd.as<float2>(), M, K, acc.as<double>(), st));
   } else {
@@ -390,8 +393,18 @@ int tbk_mu_from_blocks(int32_t M, int64_t K, const double* L, const double* Rb, 
                                                                                      acc.as<double2>());
     TBK_CHECK_LAUNCH();
   }
+  TBK_CUDA(cudaEventRecord(ev[1], st));
   TBK_CUDA(cudaMemcpyAsync(mu_out, acc.p, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, st));
   TBK_CUDA(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev[0], ev[1]);
+  for (auto& e : ev) cudaEventDestroy(e);
+  KuboTiming tm;
+  tm.ms_gemm = ms;
+  tm.gemm_flops = 8.0 * M * (double)M * (double)K * ((flags & TBK_MU_TENSOR) ? 3.0 : 1.0);
+  tm.block_bytes = 2.0 * M * (double)K * 8.0;
+  tm.chunks = 1;
+  g_kubo_timing = tm;
   return TBK_OK;
 }
 
