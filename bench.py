@@ -362,7 +362,7 @@ def peaks_tensor():
     return 1900.0 / 2.0, "half of fallback bf16"
 
 
-def run_kubo(config: int, tensor: bool = True, recursion: str = "fp64"):
+def run_kubo(config: int, tensor: bool = True, recursion: str = "dd"):
     """Kubo legs: config 3 (Bastin sigma_xy, square 256^2 open-x / periodic-y, Landau
     flux 1/64, M = 512, R = 16, seed 2) or config 5 (Greenwood sigma_xx, FCC 128^3
     periodic, on-site U[-1,1] seed 4, M = 1024, R = 8)."""
@@ -601,13 +601,13 @@ def main():
     ap.add_argument("--kernel-only", action="store_true", help="small profiling case (no e2e/fp64/cpu legs)")
     ap.add_argument("--cells", type=int, default=512)
     ap.add_argument("--moments", type=int, default=32)
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "dd"])
     ap.add_argument("--staged", action="store_true", help="TMA-staged warp-specialised kernel (A/B)")
     ap.add_argument("--kubo", type=int, default=0, choices=[0, 3, 5],
                     help="run only the Kubo leg of config 3 (sigma_xy) or 5 (sigma_xx)")
     ap.add_argument("--cuda-core-mu", action="store_true", help="Kubo leg with the CUDA-core mu GEMM")
-    ap.add_argument("--kubo-recursion", default="fp64", choices=["fp64", "mixed"],
-                    help="stored-block recursion: complex128 (default) or complex64")
+    ap.add_argument("--kubo-recursion", default="dd", choices=["fp64", "mixed", "dd"],
+                    help="stored-block recursion: double-float (default), complex128 or complex64")
     ap.add_argument("--no-hopping", action="store_true",
                     help="diagonal-only H (same vector streams, no neighbour gathers): stream ceiling")
     ap.add_argument("--serve", action="store_true", help="serving stream (config 4) instead of the DoS solve")

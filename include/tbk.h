@@ -47,7 +47,10 @@ int tbk_device_count(void);
 /* ------------------------------------------------------------ precision */
 enum {
   TBK_PREC_FP64 = 0,        /* complex128 recursion, FP64 H: the plain drop-in   */
-  TBK_PREC_MIXED = 1        /* complex64 recursion, FP32 H, FP64 moment sums     */
+  TBK_PREC_MIXED = 1,       /* complex64 recursion, FP32 H, FP64 moment sums     */
+  TBK_PREC_DD = 2           /* double-float recursion (FP32 hi + lo pairs, ~48
+                               bits) on the FP32 pipe: FP64-class accuracy at
+                               memory speed on GB300's slow FP64 pipe          */
 };
 enum {
   TBK_FLAG_PREC_MASK = 0xF,
@@ -221,8 +224,9 @@ int tbk_dos_from_moments(int32_t n, const double* mu, int32_t kernel_kind, doubl
 enum {
   TBK_MU_CUDA_CORE = 0,             /* mu_nm GEMM on CUDA cores (FP32 chunks, FP64 sums) */
   TBK_MU_TENSOR = 1,                /* mu_nm GEMM on tcgen05 (split TF32)               */
-  TBK_MU_MIXED_RECURSION = 2        /* complex64 recursion for the stored blocks (FP32
+  TBK_MU_MIXED_RECURSION = 2,       /* complex64 recursion for the stored blocks (FP32
                                        H~); default: complex128 recursion, FP64 H~      */
+  TBK_MU_DD_RECURSION = 4           /* double-float recursion for the stored blocks     */
 };
 /* mu_mn = sum_{sites,r} conj(aL_m) aR_n with aL_m = g_m AL T_m(H~) BL |r>,
  * aR_n = g_n AR T_n(H~) BR |r> (NULL operator = identity), m, n < M: the stored

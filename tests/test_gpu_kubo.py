@@ -131,6 +131,31 @@ def test_greenwood_spectrum_and_v_moments(gpu):
 
 
 @pytest.mark.parametrize("which", ["bastin", "greenwood"])
+def test_mu_nm_dd_recursion(gpu, which):
+    """double-float recursion for the stored blocks: the complex128 bound."""
+    tb = gpu
+    X, H = _system(tb)
+    G = tb.GreenFunction(32, H, -4.1, 4.1)
+    Ht = G.scaled_HE
+    v_x = tb.commutator(Ht, X.op_position(0))
+    v_y = tb.commutator(Ht, X.op_position(1))
+    n, cp, ri, v, ovx, ovy = _oracle_ops(tb, X, Ht)
+    kets = orc.random_phase_kets(n, 3, 2)
+    g = orc.kernel_seq(orc.K_LORENTZ, 32, 6.0)
+    if which == "bastin":
+        mu = tb.kubo_mu(Ht, None, None, v_x, v_y, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True, recursion="dd")
+        mu64 = tb.kubo_mu(Ht, None, None, v_x, v_y, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True)
+        ref = orc.kubo_mu(n, cp, ri, v, 32, kets, AR=ovx, BR=ovy, g=g)
+    else:
+        mu = tb.kubo_mu(Ht, v_x, v_x, None, None, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True, recursion="dd")
+        mu64 = tb.kubo_mu(Ht, v_x, v_x, None, None, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True)
+        ref = orc.kubo_mu(n, cp, ri, v, 32, kets, AL=ovx, BL=ovx, g=g)
+    assert _rel(mu, ref) <= MU_TOL, _rel(mu, ref)
+    # the blocks are rounded to complex64 either way: dd and FP64 recursions agree to that rounding
+    assert _rel(mu, mu64) <= 1e-6, _rel(mu, mu64)
+
+
+@pytest.mark.parametrize("which", ["bastin", "greenwood"])
 def test_mu_nm_mixed_recursion(gpu, which):
     """complex64 recursion (FP32 H~) for the stored blocks: same bound as the
     complex128 recursion on M = 32."""

@@ -5,6 +5,7 @@ Tolerances (stated, relative to mu_0 = Re tr(bras^dagger kets)):
   FP64 with moment doubling                     <= 1e-10
   mixed precision (complex64 recursion, FP64
   moment sums), M <= 256                        <= MIXED_TOL
+  double-float recursion (FP32 hi + lo pairs)   <= DD_TOL
 """
 import numpy as np
 import pytest
@@ -14,6 +15,7 @@ from helpers import landau_gauge, spec_from, with_onsite_zeros
 
 pytestmark = pytest.mark.gpu
 MIXED_TOL = 2e-5
+DD_TOL = 1e-10
 
 
 def _system(tb, kind="square", L=(16, 16), cplx=False, disorder=None, gauge=None):
@@ -168,3 +170,31 @@ def test_large_mixed_properties(gpu):
     assert abs(ref[0] - 32.0) < 1e-9                      # normalised kets: mu_0 = R
     assert np.all(np.abs(mu) <= 32.0 * (1 + 1e-6))         # |T_n| <= 1 on the rescaled spectrum
     assert _err(mu, ref) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("cplx,R", [(False, 8), (True, 8), (False, 32), (False, 1), (True, 40)])
+def test_dd_precision_bound(gpu, cplx, R):
+    """double-float recursion: FP64-class moments (same systems as the mixed bound)."""
+    tb = gpu
+    X, H = _system(tb, "square", (64, 64), cplx, disorder=(0.5, 7))
+    G, cp, ri, v = _rescaled_csc(tb, H, 4.5)
+    n = len(cp) - 1
+    kets = orc.random_phase_kets(n, R, 0)
+    ref = orc.cheb_moments(n, cp, ri, v, 256, kets, kets)
+    for doubling in (False, True):
+        mu = tb.Cheb_first_kind_seq_braket((n, cp, ri, v), 256, kets, kets, precision="dd", doubling=doubling)
+        assert _err(mu, ref) <= DD_TOL, (doubling, _err(mu, ref))
+
+
+def test_dd_exact_trace_golden(gpu):
+    tb = gpu
+    from pathlib import Path
+    gold = np.load(Path(__file__).resolve().parent / "golden" / "exact_moments.npz")
+    mu_exact, a = gold["honeycomb_L12_t-2.7"], float(gold["honeycomb_L12_t-2.7__a"][0])
+    X = tb.PartialLattice(tb.Honeycomb().add_hopping("A", 1, -2.7), (12, 12))
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], float)
+    G = tb.GreenFunction(len(mu_exact), H, -a, a)
+    n = H.shape[0]
+    eye = np.asfortranarray(np.eye(n, dtype=np.complex128))
+    mu = tb.KpmSolver(G.scaled_HE, n, precision="dd", doubling=False).run(len(mu_exact), eye, eye)
+    assert np.max(np.abs(mu - mu_exact)) / mu_exact[0] <= DD_TOL

@@ -25,6 +25,7 @@ TBK_PENDING = 7
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_DD = 2
 FLAG_DOUBLING = 1 << 4
 FLAG_DEVICE_PTRS = 1 << 5
 FLAG_NO_L2_ZIGZAG = 1 << 6
@@ -34,7 +35,7 @@ BUILD_SPARSE = 0
 BUILD_PERIODIC_BARE = 1
 BUILD_BARE = 2
 
-MU_CUDA_CORE, MU_TENSOR, MU_MIXED_RECURSION = 0, 1, 2
+MU_CUDA_CORE, MU_TENSOR, MU_MIXED_RECURSION, MU_DD_RECURSION = 0, 1, 2, 4
 
 KERNEL_DIRICHLET, KERNEL_FEJER, KERNEL_LORENTZ, KERNEL_JACKSON, KERNEL_LANCZOS, KERNEL_WANG_ZUNGER = range(6)
 

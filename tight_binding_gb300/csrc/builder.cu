@@ -574,6 +574,32 @@ int ensure_ell(tbk_sparse_s* A, cudaStream_t st) {
   return TBK_OK;
 }
 
+// FP64 values -> double-float (hi, lo) pairs: hi = rn(v), lo = rn(v - hi)
+__global__ void to_dd_kernel(int64_t n, const double* __restrict__ v, float2* __restrict__ out) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const double x = v[q];
+    const float h = __double2float_rn(x);
+    out[q] = make_float2(h, __double2float_rn(x - (double)h));
+  }
+}
+
+int ensure_ell_dd(tbk_sparse_s* A, cudaStream_t st) {
+  TBK_TRY(ensure_ell(A, st));
+  EllDev& E = A->ell;
+  if (E.valdd.p) return TBK_OK;
+  if (!E.val64.p || !E.diag64.p) return fail(TBK_ERR_INVALID, "double-float ELL needs the FP64 values");
+  const int64_t nv = E.val64.bytes / sizeof(double), nd = E.diag64.bytes / sizeof(double);
+  TBK_TRY(E.valdd.alloc(sizeof(float2) * nv));
+  TBK_TRY(E.diagdd.alloc(sizeof(float2) * nd));
+  to_dd_kernel<<<(unsigned)std::min<int64_t>((nv + 255) / 256, 65535), 256, 0, st>>>(nv, E.val64.as<double>(),
+                                                                                   E.valdd.as<float2>());
+  TBK_CHECK_LAUNCH();
+  to_dd_kernel<<<(unsigned)std::min<int64_t>((nd + 255) / 256, 65535), 256, 0, st>>>(nd, E.diag64.as<double>(),
+                                                                                   E.diagdd.as<float2>());
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
+}
+
 }  // namespace tbk
 
 using namespace tbk;

@@ -15,6 +15,8 @@
 //
 // Two precisions:
 //   TBK_PREC_FP64 : complex128 vectors, FP64 H~ (the plain drop-in)
+//   TBK_PREC_DD   : double-float vectors and H~ (hi + lo FP32 pairs, ~48 bits),
+//                   FP32-pipe arithmetic, per-thread double-float sums
 //   TBK_PREC_MIXED: complex64 vectors, FP32 H~, FP32 per-thread sums promoted
 //                   to FP64 for every reduction above the thread.
 // With bras == kets (DoS) the Chebyshev product rule gives two moments per step:
@@ -372,10 +374,19 @@ static int rows_per_tile(int prec, int Rc) {
 }
 
 // ---------------------------------------------------------------- internal API
-// (used by the Kubo block recursions in kubo.cu)
-int step_config(tbk_sparse_s* A, int Rc, bool fp64, int* grid, int* n_tiles, cudaStream_t st) {
+// (used by the Kubo block recursions in kubo.cu and the server)
+// ELL value arrays of a precision: FP32, FP64 or double-float pairs.
+static const void* ell_vals(const EllDev& E, int prec) {
+  return prec == TBK_PREC_MIXED ? E.val32.p : prec == TBK_PREC_DD ? E.valdd.p : E.val64.p;
+}
+static const void* ell_diag(const EllDev& E, int prec) {
+  return prec == TBK_PREC_MIXED ? E.diag32.p : prec == TBK_PREC_DD ? E.diagdd.p : E.diag64.p;
+}
+
+int step_config(tbk_sparse_s* A, int Rc, int prec, int* grid, int* n_tiles, cudaStream_t st) {
   TBK_TRY(ensure_ell(A, st));
-  const int rpt = rows_per_tile(fp64 ? TBK_PREC_FP64 : TBK_PREC_MIXED, Rc);
+  if (prec == TBK_PREC_DD) TBK_TRY(ensure_ell_dd(A, st));
+  const int rpt = rows_per_tile(prec, Rc);
   *n_tiles = (A->rows + rpt - 1) / rpt;
   int occ = 1;
   const bool cplx = A->ell.cplx != 0;
@@ -388,13 +399,13 @@ int step_config(tbk_sparse_s* A, int Rc, bool fp64, int* grid, int* n_tiles, cud
     case 16: occ = cplx ? occupancy_blocks<F, true, 16>() : occupancy_blocks<F, false, 16>(); break;     \
     default: occ = cplx ? occupancy_blocks<F, true, 32>() : occupancy_blocks<F, false, 32>(); break;     \
   }
-  if (fp64) { OCC2(double) } else { OCC2(float) }
+  if (prec == TBK_PREC_FP64) { OCC2(double) } else if (prec == TBK_PREC_DD) { OCC2(dd) } else { OCC2(float) }
 #undef OCC2
   *grid = std::max(1, std::min(*n_tiles, sm_count() * occ));
   return TBK_OK;
 }
 
-int step_any(tbk_sparse_s* A, int Rc, bool fp64, const void* x, void* y, const void* pv, bool first, double* part,
+int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
              int grid, int n_tiles, cudaStream_t st) {
   StepArgs a;
   a.n = A->rows;
@@ -403,8 +414,8 @@ int step_any(tbk_sparse_s* A, int Rc, bool fp64, const void* x, void* y, const v
   a.err = nullptr;
   a.soff = A->ell.slice_off.as<int32_t>();
   a.ecol = A->ell.col.as<int32_t>();
-  a.eval = fp64 ? A->ell.val64.p : A->ell.val32.p;
-  a.diag = fp64 ? A->ell.diag64.p : A->ell.diag32.p;
+  a.eval = ell_vals(A->ell, prec);
+  a.diag = ell_diag(A->ell, prec);
   a.x = x;
   a.y = y;
   a.pv = first ? y : pv;
@@ -414,27 +425,32 @@ int step_any(tbk_sparse_s* A, int Rc, bool fp64, const void* x, void* y, const v
   a.reverse = 0;
   a.gather = 1;
   a.pf_dist = 1;
-  if (fp64)
-    return A->ell.cplx ? launch_step<double, true>(Rc, a, first, false, grid, st)
-                         : launch_step<double, false>(Rc, a, first, false, grid, st);
-  return A->ell.cplx ? launch_step<float, true>(Rc, a, first, false, grid, st)
-                       : launch_step<float, false>(Rc, a, first, false, grid, st);
+  const bool c = A->ell.cplx != 0;
+  if (prec == TBK_PREC_FP64)
+    return c ? launch_step<double, true>(Rc, a, first, false, grid, st) : launch_step<double, false>(Rc, a, first, false, grid, st);
+  if (prec == TBK_PREC_DD)
+    return c ? launch_step<dd, true>(Rc, a, first, false, grid, st) : launch_step<dd, false>(Rc, a, first, false, grid, st);
+  return c ? launch_step<float, true>(Rc, a, first, false, grid, st) : launch_step<float, false>(Rc, a, first, false, grid, st);
 }
 
-int load_block_any(bool fp64, int32_t n, int32_t R, int32_t r0, int32_t Rp, const double2* src, void* dst,
+int load_block_any(int prec, int32_t n, int32_t R, int32_t r0, int32_t Rp, const double2* src, void* dst,
                    cudaStream_t st) {
   dim3 g((unsigned)((n + 31) / 32), (unsigned)((Rp + 31) / 32)), b(32, 8);
-  if (fp64) load_block_kernel<double><<<g, b, 0, st>>>(n, R, r0, std::min(Rp, R - r0), Rp, src, static_cast<double2*>(dst));
-  else load_block_kernel<float><<<g, b, 0, st>>>(n, R, r0, std::min(Rp, R - r0), Rp, src, static_cast<float2*>(dst));
+  const int32_t rc = std::min(Rp, R - r0);
+  if (prec == TBK_PREC_FP64) load_block_kernel<double><<<g, b, 0, st>>>(n, R, r0, rc, Rp, src, static_cast<double2*>(dst));
+  else if (prec == TBK_PREC_DD) load_block_kernel<dd><<<g, b, 0, st>>>(n, R, r0, rc, Rp, src, static_cast<dd2*>(dst));
+  else load_block_kernel<float><<<g, b, 0, st>>>(n, R, r0, rc, Rp, src, static_cast<float2*>(dst));
   TBK_CHECK_LAUNCH();
   return TBK_OK;
 }
 
-int random_block_any(bool fp64, int32_t n, int32_t R, int32_t r0, int32_t Rp, uint64_t seed, void* dst,
+int random_block_any(int prec, int32_t n, int32_t R, int32_t r0, int32_t Rp, uint64_t seed, void* dst,
                      cudaStream_t st) {
-  int64_t tot = (int64_t)n * Rp;
-  if (fp64) random_block_kernel<double><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(n, R, r0, Rp, seed, static_cast<double2*>(dst));
-  else random_block_kernel<float><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(n, R, r0, Rp, seed, static_cast<float2*>(dst));
+  const int64_t tot = (int64_t)n * Rp;
+  const unsigned g = (unsigned)((tot + 255) / 256);
+  if (prec == TBK_PREC_FP64) random_block_kernel<double><<<g, 256, 0, st>>>(n, R, r0, Rp, seed, static_cast<double2*>(dst));
+  else if (prec == TBK_PREC_DD) random_block_kernel<dd><<<g, 256, 0, st>>>(n, R, r0, Rp, seed, static_cast<dd2*>(dst));
+  else random_block_kernel<float><<<g, 256, 0, st>>>(n, R, r0, Rp, seed, static_cast<float2*>(dst));
   TBK_CHECK_LAUNCH();
   return TBK_OK;
 }
@@ -515,8 +531,8 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
       a.pf_dist = P->pf_dist;
       a.soff = E.slice_off.as<int32_t>();
       a.ecol = E.col.as<int32_t>();
-      a.eval = mixed ? E.val32.p : E.val64.p;
-      a.diag = mixed ? E.diag32.p : E.diag64.p;
+      a.eval = ell_vals(E, P->prec);
+      a.diag = ell_diag(E, P->prec);
       a.x = x;
       a.y = y;
       a.pv = y;
@@ -536,6 +552,8 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
       } else {
         if (mixed) rc = cplx ? launch_step<float, true>(P->Rc, a, first, braket, G, st)
                              : launch_step<float, false>(P->Rc, a, first, braket, G, st);
+        else if (P->prec == TBK_PREC_DD) rc = cplx ? launch_step<dd, true>(P->Rc, a, first, braket, G, st)
+                                                   : launch_step<dd, false>(P->Rc, a, first, braket, G, st);
         else rc = cplx ? launch_step<double, true>(P->Rc, a, first, braket, G, st)
                        : launch_step<double, false>(P->Rc, a, first, braket, G, st);
       }
@@ -587,9 +605,11 @@ int tbk_kpm_create(tbk_kpm* out, tbk_sparse Ht, int32_t R, int32_t flags) {
   *out = nullptr;
   if (R < 1) return fail(TBK_ERR_INVALID, "R must be >= 1");
   const int prec = flags & TBK_FLAG_PREC_MASK;
-  if (prec != TBK_PREC_FP64 && prec != TBK_PREC_MIXED) return fail(TBK_ERR_INVALID, "unknown precision %d", prec);
+  if (prec != TBK_PREC_FP64 && prec != TBK_PREC_MIXED && prec != TBK_PREC_DD)
+    return fail(TBK_ERR_INVALID, "unknown precision %d", prec);
   cudaStream_t st = nullptr;
   TBK_TRY(ensure_ell(Ht, st));
+  if (prec == TBK_PREC_DD) TBK_TRY(ensure_ell_dd(Ht, st));
   auto* P = new tbk_kpm_s();
   P->H = Ht;
   P->R = R;
@@ -616,6 +636,7 @@ int tbk_kpm_create(tbk_kpm* out, tbk_sparse Ht, int32_t R, int32_t flags) {
     default: occ = occupancy_blocks<F, C, 32>(); break;                           \
   }
   if (prec == TBK_PREC_MIXED) { if (cplx) { OCC(float, true) } else { OCC(float, false) } }
+  else if (prec == TBK_PREC_DD) { if (cplx) { OCC(dd, true) } else { OCC(dd, false) } }
   else { if (cplx) { OCC(double, true) } else { OCC(double, false) } }
 #undef OCC
   P->grid = std::max(1, std::min(P->n_tiles, sm_count() * occ));
@@ -710,6 +731,7 @@ int tbk_kpm_run(tbk_kpm P, int32_t n_mom, const double* bras, const double* kets
       dim3 g((unsigned)((P->n + 31) / 32), (unsigned)((P->Rc + 31) / 32)), b(32, 8);
       int32_t rc = std::min(P->Rc, P->R - r0);
       if (mixed) load_block_kernel<float><<<g, b, 0, st>>>((int32_t)P->n, P->R, r0, rc, P->Rc, src, static_cast<float2*>(dst));
+      else if (P->prec == TBK_PREC_DD) load_block_kernel<dd><<<g, b, 0, st>>>((int32_t)P->n, P->R, r0, rc, P->Rc, src, static_cast<dd2*>(dst));
       else load_block_kernel<double><<<g, b, 0, st>>>((int32_t)P->n, P->R, r0, rc, P->Rc, src, static_cast<double2*>(dst));
       TBK_CHECK_LAUNCH();
       return TBK_OK;
@@ -726,8 +748,8 @@ int tbk_kpm_run_random(tbk_kpm P, int32_t n_mom, uint64_t seed, double* mu_out, 
   const bool doubling = (P->flags & TBK_FLAG_DOUBLING) != 0;
   auto gen = [&](int32_t r0, void* dst) -> int {
     int64_t tot = P->n * P->Rc;
-    if (mixed) random_block_kernel<float><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>((int32_t)P->n, P->R, r0, P->Rc, seed, static_cast<float2*>(dst));
-    else random_block_kernel<double><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>((int32_t)P->n, P->R, r0, P->Rc, seed, static_cast<double2*>(dst));
+    TBK_TRY(random_block_any(P->prec, (int32_t)P->n, P->R, r0, P->Rc, seed, dst, st));
+    (void)mixed; (void)tot;
     TBK_CHECK_LAUNCH();
     return TBK_OK;
   };

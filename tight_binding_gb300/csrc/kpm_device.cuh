@@ -7,9 +7,55 @@
 
 namespace tbk {
 
+// Double-float number: value = hi + lo (|lo| <= ulp(hi) / 2), about 48
+// significant bits, computed on the FP32 pipe with error-free transformations
+// (Knuth TwoSum, Dekker / FMA TwoProduct).  On GB300 the FP64 pipe is ~64x
+// slower than FP32, so a recursion in this type runs at memory speed with
+// FP64-class accuracy.  Every step uses the _rn intrinsics so that the compiler
+// cannot contract a product and a sum into one FMA (which would break the
+// error terms).
+struct dd {
+  float hi, lo;
+  dd() = default;
+  __host__ __device__ constexpr dd(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr dd(int v) : hi((float)v), lo(0.f) {}
+  __device__ explicit dd(double v) {
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(v - (double)hi);
+  }
+  __device__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ dd dd_fast_two_sum(float a, float b) {     // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return dd(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ dd operator+(dd a, dd b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  return dd_fast_two_sum(s, e);
+}
+__device__ __forceinline__ dd operator-(dd a) { return dd(-a.hi, -a.lo); }
+__device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }
+__device__ __forceinline__ dd operator*(dd a, dd b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return dd_fast_two_sum(p, e);
+}
+__device__ __forceinline__ dd& operator+=(dd& a, dd b) { a = a + b; return a; }
+struct __align__(16) dd2 {
+  dd x, y;
+};
+
 template <typename F> struct C2;
 template <> struct C2<float> { using T = float2; };
 template <> struct C2<double> { using T = double2; };
+template <> struct C2<dd> { using T = dd2; };
+template <typename F> constexpr bool is_dd = false;
+template <> constexpr bool is_dd<dd> = true;
 
 // Lane slice of a site's R vectors: VPL complex values moved as one access.
 template <typename F, int VPL>
@@ -20,7 +66,10 @@ struct LaneV {
 template <typename F, int VPL>
 __device__ __forceinline__ LaneV<F, VPL> ld_ro(const typename C2<F>::T* p) {
   LaneV<F, VPL> o;
-  if constexpr (sizeof(F) == 4 && VPL == 2) {
+  if constexpr (is_dd<F>) {
+    float4 q = __ldg(reinterpret_cast<const float4*>(p));
+    o.re[0] = dd(q.x, q.y); o.im[0] = dd(q.z, q.w);
+  } else if constexpr (sizeof(F) == 4 && VPL == 2) {
     float4 q = __ldg(reinterpret_cast<const float4*>(p));
     o.re[0] = q.x; o.im[0] = q.y; o.re[1] = q.z; o.im[1] = q.w;
   } else {
@@ -32,7 +81,10 @@ __device__ __forceinline__ LaneV<F, VPL> ld_ro(const typename C2<F>::T* p) {
 template <typename F, int VPL>
 __device__ __forceinline__ LaneV<F, VPL> ld_stream(const typename C2<F>::T* p) {
   LaneV<F, VPL> o;
-  if constexpr (sizeof(F) == 4 && VPL == 2) {
+  if constexpr (is_dd<F>) {
+    float4 q = __ldcs(reinterpret_cast<const float4*>(p));
+    o.re[0] = dd(q.x, q.y); o.im[0] = dd(q.z, q.w);
+  } else if constexpr (sizeof(F) == 4 && VPL == 2) {
     float4 q = __ldcs(reinterpret_cast<const float4*>(p));
     o.re[0] = q.x; o.im[0] = q.y; o.re[1] = q.z; o.im[1] = q.w;
   } else {
@@ -43,7 +95,9 @@ __device__ __forceinline__ LaneV<F, VPL> ld_stream(const typename C2<F>::T* p) {
 }
 template <typename F, int VPL>
 __device__ __forceinline__ void st_v(typename C2<F>::T* p, const LaneV<F, VPL>& v) {
-  if constexpr (sizeof(F) == 4 && VPL == 2) {
+  if constexpr (is_dd<F>) {
+    *reinterpret_cast<float4*>(p) = make_float4(v.re[0].hi, v.re[0].lo, v.im[0].hi, v.im[0].lo);
+  } else if constexpr (sizeof(F) == 4 && VPL == 2) {
     *reinterpret_cast<float4*>(p) = make_float4(v.re[0], v.im[0], v.re[1], v.im[1]);
   } else {
     typename C2<F>::T q;
@@ -70,7 +124,14 @@ struct HVal;
 template <typename F>
 struct HVal<F, false> {
   F v;
-  __device__ __forceinline__ static HVal load(const F* p, int64_t o) { return HVal{__ldg(p + o)}; }
+  __device__ __forceinline__ static HVal load(const F* p, int64_t o) {
+    if constexpr (is_dd<F>) {
+      const float2 q = __ldg(reinterpret_cast<const float2*>(p) + o);
+      return HVal{dd(q.x, q.y)};
+    } else {
+      return HVal{__ldg(p + o)};
+    }
+  }
   __device__ __forceinline__ static HVal load_smem(const F* p, int32_t o) { return HVal{p[o]}; }
   __device__ __forceinline__ static HVal zero() { return HVal{F(0)}; }
   template <int VPL>
@@ -84,8 +145,13 @@ template <typename F>
 struct HVal<F, true> {
   F r, i;
   __device__ __forceinline__ static HVal load(const F* p, int64_t o) {
-    auto q = __ldg(reinterpret_cast<const typename C2<F>::T*>(p) + o);
-    return HVal{q.x, q.y};
+    if constexpr (is_dd<F>) {
+      const float4 q = __ldg(reinterpret_cast<const float4*>(p) + o);
+      return HVal{dd(q.x, q.y), dd(q.z, q.w)};
+    } else {
+      auto q = __ldg(reinterpret_cast<const typename C2<F>::T*>(p) + o);
+      return HVal{q.x, q.y};
+    }
   }
   __device__ __forceinline__ static HVal load_smem(const F* p, int32_t o) {
     auto q = reinterpret_cast<const typename C2<F>::T*>(p)[o];
@@ -105,6 +171,7 @@ struct HVal<F, true> {
 };
 
 template <typename F> struct VecW { static constexpr int max_vpl = (sizeof(F) == 4) ? 2 : 1; };
+template <> struct VecW<dd> { static constexpr int max_vpl = 1; };
 
 // Asynchronous bulk prefetch of [src, src+bytes) into L2 (no shared memory, no
 // completion to wait for); bytes % 16 == 0 and src 16-byte aligned.

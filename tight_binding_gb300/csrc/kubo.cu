@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <vector>
 
+#include "kpm_device.cuh"
 #include "tbk_internal.h"
 
 namespace tbk {
@@ -104,6 +105,7 @@ __global__ void mu_split_reduce_kernel(const double2* __restrict__ part, int32_t
 // row of the tile
 __device__ __forceinline__ float2 to_c64(double2 v) { return make_float2(__double2float_rn(v.x), __double2float_rn(v.y)); }
 __device__ __forceinline__ float2 to_c64(float2 v) { return v; }
+__device__ __forceinline__ float2 to_c64(dd2 v) { return make_float2(__fadd_rn(v.x.hi, v.x.lo), __fadd_rn(v.y.hi, v.y.lo)); }
 template <typename CT>
 __global__ void round_block_kernel(const CT* __restrict__ src, float2* __restrict__ store, int32_t m, int32_t M,
                                    int64_t n) {
@@ -250,8 +252,10 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   // near the band edges, where the Kubo weights 1/(1-e^2)^2 are largest; each
   // stored value is rounded to complex64 exactly once); TBK_MU_MIXED_RECURSION
   // runs them in complex64 with FP32 H~ (HBM-bound instead of FP64-pipe-bound).
-  const bool fp64 = (flags & TBK_MU_MIXED_RECURSION) == 0;
-  const size_t csz = fp64 ? sizeof(double2) : sizeof(float2);
+  const int prec = (flags & TBK_MU_MIXED_RECURSION) ? TBK_PREC_MIXED
+                   : (flags & TBK_MU_DD_RECURSION)  ? TBK_PREC_DD
+                                                    : TBK_PREC_FP64;
+  const size_t csz = prec == TBK_PREC_MIXED ? sizeof(float2) : sizeof(double2);
   DevBuf Ls, Rs, work, partd, part, macc, gdev, kstage;
   const int64_t blk16 = (blk + 15) / 16 * 16;           // K padded to whole 16-element tiles (zeros)
   TBK_TRY(Ls.alloc(sizeof(float2) * blk16 * M));
@@ -267,22 +271,23 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     TBK_CUDA(cudaMemcpyAsync(kstage.p, kets, sizeof(double2) * (size_t)n * R, cudaMemcpyHostToDevice, st));
   }
   int grid = 1, n_tiles = 1;
-  TBK_TRY(step_config(Ht, Rc, fp64, &grid, &n_tiles, st));
+  TBK_TRY(step_config(Ht, Rc, prec, &grid, &n_tiles, st));
   int gmax = grid;
   for (auto* o : ops)
-    if (o) { int g2, t2; TBK_TRY(step_config(o, Rc, fp64, &g2, &t2, st)); gmax = std::max(gmax, g2); }
+    if (o) { int g2, t2; TBK_TRY(step_config(o, Rc, prec, &g2, &t2, st)); gmax = std::max(gmax, g2); }
   TBK_TRY(partd.alloc(sizeof(double) * 2 * gmax));
   char* wb = work.as<char>();
   auto wblk = [&](int i) { return static_cast<void*>(wb + (size_t)i * blk * csz); };
   void* v0 = wblk(5);
   auto apply = [&](tbk_sparse_s* A, const void* x, void* y) -> int {   // y = A x
     int g, t;
-    TBK_TRY(step_config(A, Rc, fp64, &g, &t, st));
-    return step_any(A, Rc, fp64, x, y, nullptr, true, partd.as<double>(), g, t, st);
+    TBK_TRY(step_config(A, Rc, prec, &g, &t, st));
+    return step_any(A, Rc, prec, x, y, nullptr, true, partd.as<double>(), g, t, st);
   };
   auto round_to = [&](const void* src, float2* store, int32_t m) -> int {
     const unsigned g = (unsigned)std::min<int64_t>((blk + 255) / 256, 65535);
-    if (fp64) round_block_kernel<double2><<<g, 256, 0, st>>>(static_cast<const double2*>(src), store, m, M, blk);
+    if (prec == TBK_PREC_FP64) round_block_kernel<double2><<<g, 256, 0, st>>>(static_cast<const double2*>(src), store, m, M, blk);
+    else if (prec == TBK_PREC_DD) round_block_kernel<dd2><<<g, 256, 0, st>>>(static_cast<const dd2*>(src), store, m, M, blk);
     else round_block_kernel<float2><<<g, 256, 0, st>>>(static_cast<const float2*>(src), store, m, M, blk);
     TBK_CHECK_LAUNCH();
     return TBK_OK;
@@ -298,7 +303,7 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
       if (m >= 1) {
         const void* x = r[(m - 1) % 3];
         const void* pv = m >= 2 ? r[(m - 2) % 3] : nullptr;
-        TBK_TRY(step_any(Ht, Rc, fp64, x, y, pv, m == 1, partd.as<double>(), grid, n_tiles, st));
+        TBK_TRY(step_any(Ht, Rc, prec, x, y, pv, m == 1, partd.as<double>(), grid, n_tiles, st));
       }
       if (Aout) { TBK_TRY(apply(Aout, y, tmpA)); TBK_TRY(round_to(tmpA, store, m)); }
       else TBK_TRY(round_to(y, store, m));
@@ -314,8 +319,8 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   KuboTiming tm;
   for (int32_t r0 = 0; r0 < R; r0 += Rc) {
     TBK_CUDA(cudaEventRecord(ev[0], st));
-    if (kets) TBK_TRY(load_block_any(fp64, n, R, r0, Rc, kstage.as<double2>(), v0, st));
-    else TBK_TRY(random_block_any(fp64, n, R, r0, Rc, seed, v0, st));
+    if (kets) TBK_TRY(load_block_any(prec, n, R, r0, Rc, kstage.as<double2>(), v0, st));
+    else TBK_TRY(random_block_any(prec, n, R, r0, Rc, seed, v0, st));
     TBK_TRY(side(AL, BL, Ls.as<float2>()));
     TBK_TRY(side(AR, BR, Rs.as<float2>()));
     TBK_CUDA(cudaEventRecord(ev[1], st));

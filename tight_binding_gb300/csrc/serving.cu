@@ -600,7 +600,7 @@ int build_request(tbk_server_s* S, SrvRequest* r) {
     TBK_TRY(r->vec[2 * c + 1].alloc(blk));
     TBK_CUDA(cudaMemsetAsync(r->vec[2 * c].p, 0, blk, st));
     TBK_CUDA(cudaMemsetAsync(r->vec[2 * c + 1].p, 0, blk, st));
-    TBK_TRY(random_block_any(!mixed, r->n, q.R, c * r->rc, r->rc, q.seed, r->vec[2 * c].p, st));
+    TBK_TRY(random_block_any(q.precision, r->n, q.R, c * r->rc, r->rc, q.seed, r->vec[2 * c].p, st));
   }
   TBK_TRY(r->sums.alloc(sizeof(double) * 2 * (size_t)r->n_steps));
   TBK_CUDA(cudaStreamSynchronize(st));
@@ -985,7 +985,7 @@ int autotune(tbk_server_s* S) {
                                                                      eval.as<double>(), diag.as<double>());
       TBK_CUDA(cudaGetLastError());
       TBK_CUDA(cudaMemsetAsync(vb.p, 0, vb.bytes, st));
-      TBK_TRY(random_block_any(prec == TBK_PREC_FP64, n, rc, 0, rc, 7, va.p, st));
+      TBK_TRY(random_block_any(prec, n, rc, 0, rc, 7, va.p, st));
       // table: one lane at step 1 of a long recursion, all its slabs in group `code`
       const size_t off_l = (sizeof(SHdr) + 255) & ~(size_t)255, off_s = off_l + ((sizeof(SLane) + 255) & ~(size_t)255);
       std::vector<char> h(off_s + sizeof(SSlab) * (size_t)n_slab, 0);

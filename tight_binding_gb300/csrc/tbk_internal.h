@@ -97,6 +97,8 @@ struct EllDev {
   DevBuf diag64;      // double / double2 [n_rows]
   DevBuf val32;       // float / float2 [n_entries]  (mixed precision)
   DevBuf diag32;      // float / float2 [n_rows]
+  DevBuf valdd;       // double-float (hi, lo) pairs, real or complex [n_entries] (on demand)
+  DevBuf diagdd;      // [n_rows]
 };
 
 }  // namespace tbk
@@ -117,17 +119,19 @@ struct tbk_sparse_s {
 namespace tbk {
 // builder.cu
 int ensure_ell(tbk_sparse_s* A, cudaStream_t st);
+int ensure_ell_dd(tbk_sparse_s* A, cudaStream_t st);   // double-float copy of the FP64 values
 int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t st, int32_t* total_host);
 int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st, int64_t* total_host);
 int sm_count();
-// kpm.cu — one fused recursion step with the one-pass kernel (complex64 or
-// complex128 vectors): y = H x (first) or y = 2 H x - pv; moment partials into
-// part[2 * grid].  Block loaders: Eigen-layout kets / seeded random phases.
-int step_config(tbk_sparse_s* A, int Rc, bool fp64, int* grid, int* n_tiles, cudaStream_t st);
-int step_any(tbk_sparse_s* A, int Rc, bool fp64, const void* x, void* y, const void* pv, bool first, double* part,
+// kpm.cu — one fused recursion step with the one-pass kernel in a precision
+// TBK_PREC_* (complex64, complex128 or double-float vectors): y = H x (first)
+// or y = 2 H x - pv; moment partials into part[2 * grid].  Block loaders:
+// Eigen-layout kets / seeded random phases.
+int step_config(tbk_sparse_s* A, int Rc, int prec, int* grid, int* n_tiles, cudaStream_t st);
+int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
              int grid, int n_tiles, cudaStream_t st);
-int load_block_any(bool fp64, int32_t n, int32_t R, int32_t r0, int32_t Rp, const double2* src, void* dst,
+int load_block_any(int prec, int32_t n, int32_t R, int32_t r0, int32_t Rp, const double2* src, void* dst,
                    cudaStream_t st);
-int random_block_any(bool fp64, int32_t n, int32_t R, int32_t r0, int32_t Rp, uint64_t seed, void* dst,
+int random_block_any(int prec, int32_t n, int32_t R, int32_t r0, int32_t Rp, uint64_t seed, void* dst,
                      cudaStream_t st);
 }  // namespace tbk

@@ -19,7 +19,7 @@ from . import capi
 from .capi import check, lib
 from .lattice import PartialLattice, SparseMatrix
 
-PREC = {"fp64": capi.PREC_FP64, "mixed": capi.PREC_MIXED}
+PREC = {"fp64": capi.PREC_FP64, "mixed": capi.PREC_MIXED, "dd": capi.PREC_DD}
 
 
 def _prec(p) -> int:
