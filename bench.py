@@ -321,6 +321,22 @@ def run_gpu(args):
     mu64 = mu64_d.cpu().numpy()
     mixed_vs_fp64 = float(np.max(np.abs(mu[:m64] - mu64)) / abs(mu64[0]))
     ms64, nl64, b64 = fp.last_timing()
+    del fp
+
+    # ---- double-float plain path: the same algorithm with FP64-class accuracy on the FP32 pipe
+    ddp = tb.KpmSolver(Ht, R_VEC, precision="dd", doubling=False, flags=capi.FLAG_DEVICE_PTRS)
+    with torch.cuda.stream(stream):
+        ddp.run_device(m64, kets_d.data_ptr(), kets_d.data_ptr(), mu64_d.data_ptr(), sh)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    with torch.cuda.stream(stream):
+        ddp.run_device(m64, kets_d.data_ptr(), kets_d.data_ptr(), mu64_d.data_ptr(), sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dd_ms = e0.elapsed_time(e1)
+    mudd = mu64_d.cpu().numpy()
+    msdd, nldd, bdd = ddp.last_timing()
+    del ddp
 
     # ---- CPU baseline: oracle on a bounded sample (all host cores)
     threads = os.cpu_count() or 1
@@ -344,6 +360,9 @@ def run_gpu(args):
         "fp64_plain": {"value": fp_value, "unit": UNIT, "moments": m64, "ms": fp_ms,
                        "kernel_ms": ms64, "launches": nl64, "bytes_per_launch": b64,
                        "speedup_mixed_over_fp64": value / fp_value},
+        "dd_plain": {"value": float(N) * m64 * R_VEC / (dd_ms / 1e3), "unit": UNIT, "moments": m64, "ms": dd_ms,
+                     "kernel_GBps": bdd * nldd / (msdd / 1e3) / 1e9, "speedup_over_fp64_plain": fp_ms / dd_ms,
+                     "rel_err_vs_fp64": float(np.max(np.abs(mudd - mu64)) / abs(mu64[0]))},
         "parity": {"mixed_vs_fp64_rel_err_first_%d_moments" % m64: mixed_vs_fp64, "e2e_vs_resident_rel": e2e_err},
     }
     print(json.dumps(line), flush=True)
