@@ -1,0 +1,123 @@
+// C++ use of the kernel-polynomial path through include/tbk.hpp, written the
+// way the reference's own drivers use its API (TB/functions.h, TB/snippets.h).
+// Prints one line per check and exits non-zero on the first failure.
+//   1. ring of 96 sites, t = 1, periodic: moments with identity kets against
+//      the exact traces sum_k T_n(2 cos(2 pi k / N) / a)  (FP64, DD: 1e-10;
+//      mixed: 2e-5 of mu_0)
+//   2. n < 2 is rejected with the reference's message
+//   3. density_of_states_seq on a disordered square lattice: non-negative on
+//      the grid, integrates to ~1 (trapezoid), matches the DCT-III route
+//   4. bras != kets (plain braket) equals bras == kets (doubling) on the same
+//      kets to 1e-12
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+
+#include "tbk.hpp"
+
+using namespace tbk;
+
+static int failures = 0;
+static void expect(bool ok, const char* what, double value) {
+  std::printf("%s %s (%.3g)\n", ok ? "PASS" : "FAIL", what, value);
+  if (!ok) ++failures;
+}
+
+int main() {
+  if (tbk_device_count() < 1) {
+    std::printf("FAIL no CUDA device\n");
+    return 2;
+  }
+  const double pi = 3.14159265358979323846;
+  // ---- 1. ring: exact traces
+  {
+    const int L = 96, M = 64;
+    UnitCell<1> chain({{1, 0, 0}}, {{"A", {0, 0, 0}}});
+    chain.add_hopping("A", 1, Complex(1.0, 0.0));
+    PartialLattice<1> X(chain, {L});
+    SparseMatrix H = X.get_Hamiltonian_periodic_extend_bare_sparse<double>({1});
+    const double a = 2.05;
+    GreenFunction G(M, H, -a, a);
+    std::vector<double> exact(M, 0.0);
+    for (int k = 0; k < L; ++k) {
+      const double th = std::acos(2.0 * std::cos(2 * pi * k / L) / a);
+      for (int n = 0; n < M; ++n) exact[n] += std::cos(n * th);
+    }
+    MatrixXcd eye = MatrixXcd::Identity(L);
+    for (int prec : {TBK_PREC_FP64, TBK_PREC_DD, TBK_PREC_MIXED}) {
+      auto mu = cuda::Cheb_first_kind_seq_braket(G.scaled_HE, M, eye, eye, prec);
+      double err = 0.0;
+      for (int n = 0; n < M; ++n) err = std::fmax(err, std::fabs(mu[n] - exact[n]) / L);
+      const double tol = prec == TBK_PREC_MIXED ? 2e-5 : 1e-10;
+      const std::string what = std::string("ring exact traces, precision ") + std::to_string(prec);
+      expect(err <= tol, what.c_str(), err);
+    }
+  }
+  // ---- 2. the reference's n >= 2 rule
+  {
+    UnitCell<1> chain({{1, 0, 0}}, {{"A", {0, 0, 0}}});
+    chain.add_hopping("A", 1, Complex(1.0, 0.0));
+    PartialLattice<1> X(chain, {8});
+    SparseMatrix H = X.get_Hamiltonian_periodic_extend_bare_sparse<double>({1});
+    MatrixXcd k = bases_of_uniform_ampl_with_random_phases(8, 2, 1);
+    bool threw = false;
+    try {
+      cuda::Cheb_first_kind_seq_braket(H, 1, k, k);
+    } catch (const std::invalid_argument& e) {
+      threw = std::string(e.what()).find("n must be greater than or equal to 2") != std::string::npos;
+    }
+    expect(threw, "n < 2 rejected with the reference's message", 0.0);
+  }
+  // ---- 3. DoS of a disordered square lattice
+  {
+    UnitCell<2> square({{1, 0, 0}, {0, 1, 0}}, {{"A", {0, 0, 0}}});
+    square.add_hopping("A", 1, Complex(1.0, 0.0));
+    PartialLattice<2> X(square, {48, 48});
+    X.set_scalar_disorder(1.0, 5);
+    const int N = 256;
+    std::vector<double> e_list;
+    for (int i = 0; i < 801; ++i) e_list.push_back(-0.998 + 1.996 * i / 800.0);
+    auto dos = density_of_states_seq<double>(X, N, e_list, -4.6, 4.6, 8, 3);
+    double mn = 1e30, integral = 0.0;
+    for (size_t i = 0; i < dos.size(); ++i) {
+      mn = std::fmin(mn, dos[i]);
+      if (i) integral += 0.5 * (dos[i] + dos[i - 1]) * (e_list[i] - e_list[i - 1]);
+    }
+    expect(mn > -1e-3, "DoS non-negative on the grid", mn);
+    expect(std::fabs(integral - 1.0) < 2e-2, "DoS integrates to 1 (scaled units)", integral);
+    // the same moments through the DCT-III route at its nodes: it returns
+    // sum (2 - d_n0) g_n mu_n T_n(x) / sqrt(1 - x^2) = -f(x), since
+    // Im alpha_n(x) = -(2 - d_n0) T_n(x) / sqrt(1 - x^2)
+    SparseMatrix H = X.get_Hamiltonian_periodic_extend_bare_sparse<double>({1, 1});
+    GreenFunction G(N, H, -4.6 - 1e-8, 4.6 + 1e-8);
+    MatrixXcd kets = bases_of_uniform_ampl_with_random_phases(X.get_total_number(), 8, 3);
+    auto f = G.imag(kets, kets);
+    auto ev = f.fft(1);
+    double diff = 0.0, scale = 0.0;
+    for (int i = 0; i < N; i += 17) {
+      diff = std::fmax(diff, std::fabs(ev.second[i] + f(ev.first[i])));
+      scale = std::fmax(scale, std::fabs(ev.second[i]));
+    }
+    expect(diff <= 1e-9 * scale, "DCT-III route equals direct evaluation", diff / scale);
+  }
+  // ---- 4. plain braket vs doubling
+  {
+    UnitCell<2> hc({{1.5, -0.8660254037844386, 0}, {1.5, 0.8660254037844386, 0}}, {{"A", {0, 0, 0}}, {"B", {1, 0, 0}}});
+    hc.add_hopping("A", 1, Complex(-2.7, 0.0));
+    PartialLattice<2> X(hc, {24, 24});
+    X.set_scalar_disorder(0.8, 2);
+    SparseMatrix H = X.get_Hamiltonian_periodic_extend_bare_sparse<double>({1, 1});
+    GreenFunction G(100, H, -8.7, 8.7);
+    MatrixXcd k1 = bases_of_uniform_ampl_with_random_phases(X.get_total_number(), 6, 9);
+    MatrixXcd k2 = k1;                                   // distinct object: plain braket path
+    auto mu_d = cuda::Cheb_first_kind_seq_braket(G.scaled_HE, 100, k1, k1);
+    auto mu_p = cuda::Cheb_first_kind_seq_braket(G.scaled_HE, 100, k2, k1);
+    double err = 0.0;
+    for (int n = 0; n < 100; ++n) err = std::fmax(err, std::fabs(mu_d[n] - mu_p[n]) / mu_p[0]);
+    expect(err < 1e-12, "doubling equals the plain braket (FP64)", err);
+  }
+  std::printf("%s\n", failures ? "FAILED" : "ALL PASSED");
+  return failures ? 1 : 0;
+}

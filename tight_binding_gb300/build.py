@@ -81,6 +81,19 @@ def build_library(verbose: bool = False) -> Path:
     return LIB
 
 
+CPP_TEST = ROOT / "tests" / "cpp" / "test_tbk_cpp.cpp"
+CPP_TEST_BIN = OUT / "test_tbk_cpp"
+
+
+def build_cpp_test() -> Path:
+    """The C++ program that drives the path through include/tbk.hpp (run by a GPU test)."""
+    deps = [CPP_TEST, ROOT / "include" / "tbk.hpp", ROOT / "include" / "tbk.h", LIB]
+    if _stale(CPP_TEST_BIN, deps):
+        _run([os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-I", str(ROOT / "include"),
+              str(CPP_TEST), "-L", str(OUT), "-ltbk", "-Wl,-rpath,$ORIGIN", "-o", str(CPP_TEST_BIN)])
+    return CPP_TEST_BIN
+
+
 def build_oracle() -> Path:
     _run(["make", "-s", "-C", str(ROOT / "oracle")])
     return ROOT / "oracle" / "_build" / "libkpm_oracle.so"
@@ -88,6 +101,7 @@ def build_oracle() -> Path:
 
 def build_all(verbose: bool = False) -> None:
     build_library(verbose)
+    build_cpp_test()
     build_oracle()
 
 
