@@ -599,12 +599,12 @@ def run_kernel_only(args):
     G = tb.GreenFunction(args.moments, H, -BOUND, BOUND)
     from tight_binding_gb300 import capi
 
-    flags = capi.FLAG_STAGED if args.staged else 0
+    flags = (capi.FLAG_STAGED if args.staged else 0) | (capi.FLAG_TWO_STEP if args.two_step else 0)
     s = tb.KpmSolver(G.scaled_HE, R_VEC, precision=args.precision, doubling=args.precision == "mixed", flags=flags)
     for _ in range(2):
         mu = s.run_random(args.moments, 0)
     ms, nl, b = s.last_timing()
-    print(json.dumps({"staged": args.staged, "no_hopping": args.no_hopping, "precision": args.precision, "cells": args.cells, "sites": H.shape[0], "moments": args.moments, "launches": nl,
+    print(json.dumps({"staged": args.staged, "two_step": args.two_step, "no_hopping": args.no_hopping, "precision": args.precision, "cells": args.cells, "sites": H.shape[0], "moments": args.moments, "launches": nl,
                       "ms": ms, "bytes_per_launch": b, "GBps": b * nl / (ms / 1e3) / 1e9, "mu0": mu[0]}))
     return 0
 
@@ -622,6 +622,7 @@ def main():
     ap.add_argument("--moments", type=int, default=32)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "dd"])
     ap.add_argument("--staged", action="store_true", help="TMA-staged warp-specialised kernel (A/B)")
+    ap.add_argument("--two-step", action="store_true", help="two recursion steps per pass (A/B)")
     ap.add_argument("--kubo", type=int, default=0, choices=[0, 3, 5],
                     help="run only the Kubo leg of config 3 (sigma_xy) or 5 (sigma_xx)")
     ap.add_argument("--cuda-core-mu", action="store_true", help="Kubo leg with the CUDA-core mu GEMM")

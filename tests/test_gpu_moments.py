@@ -198,3 +198,23 @@ def test_dd_exact_trace_golden(gpu):
     eye = np.asfortranarray(np.eye(n, dtype=np.complex128))
     mu = tb.KpmSolver(G.scaled_HE, n, precision="dd", doubling=False).run(len(mu_exact), eye, eye)
     assert np.max(np.abs(mu - mu_exact)) / mu_exact[0] <= DD_TOL
+
+
+def test_two_step_passes_match_single_steps(gpu):
+    """TBK_FLAG_TWO_STEP (two recursion steps per pass, temporal blocking): the
+    vectors are the same bits as one step per pass (same per-row arithmetic);
+    the moments differ only by the order of the FP32 per-thread sums."""
+    tb = gpu
+    X, H = _system(tb, "honeycomb", (256, 256), False, disorder=(1.0, 1))
+    G, cp, ri, v = _rescaled_csc(tb, H, 8.7)
+    Ht = G.scaled_HE
+    two = tb.capi.FLAG_TWO_STEP
+    for M in (128, 130, 3):
+        fused = tb.KpmSolver(Ht, 32, precision="mixed", doubling=True, flags=two).run_random(M, 5)
+        single = tb.KpmSolver(Ht, 32, precision="mixed", doubling=True).run_random(M, 5)
+        assert _err(fused, single) <= 1e-6, (M, _err(fused, single))
+    n = len(cp) - 1
+    kets = orc.random_phase_kets(n, 32, 5)
+    ref = orc.cheb_moments(n, cp, ri, v, 130, kets, kets)
+    mu = tb.KpmSolver(Ht, 32, precision="mixed", doubling=True, flags=two).run_random(130, 5)
+    assert _err(mu, ref) <= MIXED_TOL, _err(mu, ref)

@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
 
 }  // namespace tbk
 #include "kpm_tma.cuh"
+#include "kpm_fused.cuh"
 namespace tbk {
 
 // Column-major complex128 (Eigen) -> site-major work block of width Rp.
@@ -476,6 +477,10 @@ struct tbk_kpm_s {
   double last_ms = 0.0, last_bytes = 0.0;
   int32_t last_launches = 0;
   int32_t cap_steps = 0;            // partial buffer capacity (steps)
+  // two-step passes (mixed precision, doubling): dependency tiles, deferred list, lag
+  bool fused = false;
+  int32_t lag = 0, n_def = 0, n_waves = 0, tpt = 4, n_tasks = 0;
+  DevBuf dep, isdef, deflist, wave;
 };
 
 static int plan_partials(tbk_kpm_s* P, int32_t n_steps) {
@@ -489,6 +494,101 @@ static int plan_partials(tbk_kpm_s* P, int32_t n_steps) {
 static int plan_mu(tbk_kpm_s* P, int32_t n_mom) {
   if (P->mu.bytes >= sizeof(double) * (size_t)n_mom) return TBK_OK;
   return P->mu.alloc(sizeof(double) * n_mom);
+}
+
+template <int R, bool C>
+static void* fused_fn() { return reinterpret_cast<void*>(kpm_fused2_kernel<R, C>); }
+static void* fused_kernel_ptr(int Rc, bool cplx) {
+  switch (Rc) {
+    case 1: return cplx ? fused_fn<1, true>() : fused_fn<1, false>();
+    case 2: return cplx ? fused_fn<2, true>() : fused_fn<2, false>();
+    case 4: return cplx ? fused_fn<4, true>() : fused_fn<4, false>();
+    case 8: return cplx ? fused_fn<8, true>() : fused_fn<8, false>();
+    case 16: return cplx ? fused_fn<16, true>() : fused_fn<16, false>();
+    case 32: return cplx ? fused_fn<32, true>() : fused_fn<32, false>();
+    case 64: return cplx ? fused_fn<64, true>() : fused_fn<64, false>();
+  }
+  return nullptr;
+}
+
+// Two-step passes: per-tile dependencies, far-reaching (wrap-around) tiles
+// deferred, lag = the widest remaining reach + two waves of the grid.  Leaves
+// P->fused false when the matrix does not suit (too many far tiles, lag >= size).
+static int plan_fused(tbk_kpm_s* P, cudaStream_t st) {
+  if (P->prec != TBK_PREC_MIXED || !(P->flags & TBK_FLAG_DOUBLING) || (P->flags & TBK_FLAG_STAGED) ||
+      !(P->flags & TBK_FLAG_TWO_STEP))
+    return TBK_OK;
+  const EllDev& E = P->H->ell;
+  const bool cplx = E.cplx != 0;
+  void* fn = fused_kernel_ptr(P->Rc, cplx);
+  if (!fn || P->n_tiles < 1) return TBK_OK;
+  int occ = 0;
+  TBK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kStepThreads, 0));
+  if (occ < 1) return TBK_OK;
+  int tpt = 4;                                          // base tiles per task
+  if (const char* e = getenv("TBK_FUSE_TILES")) tpt = std::max(1, atoi(e));   // tuning override
+  const int rpt = rows_per_tile(P->prec, P->Rc) * tpt;
+  const int32_t nt = (int32_t)((P->n + rpt - 1) / rpt);   // tasks
+  const int G = std::max(1, std::min(nt, std::min(P->grid, sm_count() * occ)));
+  TBK_TRY(P->dep.alloc(sizeof(int32_t) * nt));
+  iota_kernel<<<(nt + 255) / 256, 256, 0, st>>>(nt, P->dep.as<int32_t>());
+  TBK_CHECK_LAUNCH();
+  tile_dep_kernel<<<(unsigned)((P->n + 255) / 256), 256, 0, st>>>((int32_t)P->n, rpt, E.slice_off.as<int32_t>(),
+                                                                  E.col.as<int32_t>(), P->dep.as<int32_t>());
+  TBK_CHECK_LAUNCH();
+  std::vector<int32_t> dep(nt);
+  TBK_CUDA(cudaMemcpyAsync(dep.data(), P->dep.p, sizeof(int32_t) * nt, cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  const int32_t far = 8 * G;
+  std::vector<uint8_t> isdef(nt, 0);
+  std::vector<int32_t> defl;
+  int32_t reach = 0;
+  for (int32_t j = 0; j < nt; ++j) {
+    const int32_t d = dep[j] - j;
+    if (d > far) { isdef[j] = 1; defl.push_back(j); }
+    else reach = std::max(reach, d);
+  }
+  const int32_t lag = reach + G + G / 2;
+  if ((int64_t)defl.size() * 8 > nt || lag >= nt) return TBK_OK;
+  TBK_TRY(P->isdef.alloc(nt));
+  TBK_CUDA(cudaMemcpyAsync(P->isdef.p, isdef.data(), nt, cudaMemcpyHostToDevice, st));
+  TBK_TRY(P->deflist.alloc(sizeof(int32_t) * (defl.size() + 1)));
+  if (!defl.empty())
+    TBK_CUDA(cudaMemcpyAsync(P->deflist.p, defl.data(), sizeof(int32_t) * defl.size(), cudaMemcpyHostToDevice, st));
+  P->n_waves = (nt + G - 1) / G;
+  TBK_TRY(P->wave.alloc(sizeof(unsigned int) * P->n_waves));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  P->lag = lag;
+  P->tpt = tpt;
+  P->n_tasks = nt;
+  P->n_def = (int32_t)defl.size();
+  P->grid = G;                                          // both kernels write partials for this grid
+  P->fused = true;
+  return TBK_OK;
+}
+
+static int launch_fused(tbk_kpm_s* P, void* A, void* B, double* part1, double* part2, bool first, bool dot2,
+                        cudaStream_t st) {
+  const EllDev& E = P->H->ell;
+  void* fn = fused_kernel_ptr(P->Rc, E.cplx != 0);
+  TBK_CUDA(cudaMemsetAsync(P->wave.p, 0, sizeof(unsigned int) * P->n_waves, st));
+  int32_t n = (int32_t)P->n, nt = P->n_tasks, tpt = P->tpt, ndef = P->n_def, lag = P->lag;
+  const int32_t* soff = E.slice_off.as<int32_t>();
+  const int32_t* ecol = E.col.as<int32_t>();
+  const float* ev = E.val32.as<float>();
+  const float* dg = E.diag32.as<float>();
+  float2* a = static_cast<float2*>(A);
+  float2* b = static_cast<float2*>(B);
+  const int32_t* dep = P->dep.as<int32_t>();
+  const uint8_t* isdef = P->isdef.as<uint8_t>();
+  const int32_t* defl = P->deflist.as<int32_t>();
+  unsigned int* wave = P->wave.as<unsigned int>();
+  int fi = first ? 1 : 0, d2 = dot2 ? 1 : 0;
+  int* err = P->err.as<int>();
+  void* args[] = {&n, &nt, &tpt, &soff, &ecol, &ev, &dg, &a, &b, &dep, &isdef, &defl, &ndef, &lag, &wave, &part1,
+                  &part2, &fi, &d2, &err};
+  TBK_CUDA(cudaLaunchCooperativeKernel(fn, dim3(P->grid), dim3(kStepThreads), args, 0, st));
+  return TBK_OK;
 }
 
 // Runs all chunks.  kets_loader(r0, dst) fills the chunk's v0 (site-major);
@@ -522,7 +622,18 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
     TBK_CUDA(cudaEventRecord(P->ev0, st));
     void* x = P->va.p;
     void* y = P->vb.p;
-    for (int32_t s = 0; s < n_steps; ++s) {
+    int32_t s = 0;
+    if (doubling && P->fused && !tma) {
+      // pairs of steps per pass: x keeps v_s (then v_{s+2}), y keeps v_{s-1} (then v_{s+1})
+      for (; s + 1 < n_steps; s += 2) {
+        double* p1 = P->part.as<double>() + (((int64_t)ch * n_steps + s) * 2) * G;
+        double* p2 = P->part.as<double>() + (((int64_t)ch * n_steps + s + 1) * 2) * G;
+        const bool dot2 = s + 1 == n_steps - 1;
+        TBK_TRY(launch_fused(P, x, y, p1, p2, s == 0, dot2, st));
+        ++launches;
+      }
+    }
+    for (; s < n_steps; ++s) {
       StepArgs a;
       a.n = (int32_t)P->n;
       a.n_tiles = tma ? P->tiles_tma : P->n_tiles;
@@ -584,7 +695,16 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
   const double hv = (mixed ? 4.0 : 8.0) * (cplx ? 2.0 : 1.0);
   const double mat = (double)E.n_entries * (4.0 + hv) + (double)E.n_rows * hv + 4.0 * (E.n_slices + 1);
   double per_chunk = 0.0;
-  for (int32_t s = 0; s < n_steps; ++s) {
+  int32_t s0 = 0;
+  if (doubling && P->fused && !tma) {
+    // a pass reads v_s, v_{s-1} and H~ once and writes v_{s+1}, v_{s+2}; v_{s+1}
+    // and v_s are read again from L2 by the second step
+    for (; s0 + 1 < n_steps; s0 += 2) {
+      const bool dot2 = s0 + 1 == n_steps - 1;
+      per_chunk += (s0 > 0 ? 2 : 1) * vec + vec + (dot2 ? 0.0 : vec) + mat;
+    }
+  }
+  for (int32_t s = s0; s < n_steps; ++s) {
     const bool last_dot = doubling && s == n_steps - 1 && s > 0;
     double b = vec;                                        // x
     if (s > 0) b += vec;                                   // v_{n-1}
@@ -689,6 +809,10 @@ int tbk_kpm_create(tbk_kpm* out, tbk_sparse Ht, int32_t R, int32_t flags) {
   if (cudaEventCreate(&P->ev0) != cudaSuccess || cudaEventCreate(&P->ev1) != cudaSuccess) {
     delete P;
     return fail(TBK_ERR_CUDA, "cudaEventCreate failed");
+  }
+  if ((s = plan_fused(P, st)) != TBK_OK) {
+    delete P;
+    return s;
   }
   *out = P;
   return TBK_OK;
