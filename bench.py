@@ -518,7 +518,8 @@ def run_serve(args):
         "value": len(mine) / wall, "unit": "requests/s",
         "n_gpus": ws, "steps": len(mine), "warmup": 0, "ms_per_step": 1e3 * wall / len(mine),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64" if args.serve_precision == "mixed" else "c128", "data": "synthetic",
+        "dtype": {"mixed": "c64", "fp64": "c128", "dd": "double-float c128"}[args.serve_precision],
+        "data": "synthetic",
         "config": {"workload": f"{args.serve_requests} DoS requests, Poisson arrivals mean gap "
                                f"{args.serve_gap_ms} ms (seed 3); square/honeycomb/Kagome/Lieb L~U{{32..512}}, "
                                f"FCC L~U{{16..64}}; NN t=1.0 + disorder W~U[0,2]; M in {{256,512,1024}}; "
@@ -633,7 +634,7 @@ def main():
     ap.add_argument("--serve", action="store_true", help="serving stream (config 4) instead of the DoS solve")
     ap.add_argument("--serve-requests", type=int, default=4096)
     ap.add_argument("--serve-gap-ms", type=float, default=2.0)
-    ap.add_argument("--serve-precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--serve-precision", default="mixed", choices=["mixed", "fp64", "dd"])
     ap.add_argument("--serve-budget-gb", type=float, default=120.0)
     ap.add_argument("--serve-round", type=int, default=16)
     ap.add_argument("--serve-step-gb", type=float, default=2.0)

@@ -46,7 +46,7 @@ namespace {
 constexpr int kSrvThreads = 256;
 constexpr int kSrvWarps = kSrvThreads / 32;
 constexpr int kIterPerSlab = 8;        // warp iterations (512 B of v_s each) per slab
-constexpr int kGroups = 32;         // group code = (prec * 8 + log2(width)) * 2 + complex
+constexpr int kGroups = 48;         // group code = (prec * 8 + log2(width)) * 2 + complex, prec < 3
 
 struct SLane {                      // up to 64 vectors of one request (device view)
   const int32_t* soff;
@@ -350,6 +350,7 @@ GroupFns group_fns(int code) {
   const int rc = code_width(code);
   const bool c = code_cplx(code);
   if (code_prec(code) == TBK_PREC_MIXED) return c ? fns_for<float, true>(rc) : fns_for<float, false>(rc);
+  if (code_prec(code) == TBK_PREC_DD) return c ? fns_for<dd, true>(rc) : fns_for<dd, false>(rc);
   return c ? fns_for<double, true>(rc) : fns_for<double, false>(rc);
 }
 int width_for(int prec, int R) {
@@ -370,7 +371,7 @@ int check_request(const tbk_request* q) {
   if (!q || !q->lattice) return fail(TBK_ERR_INVALID, "request: null argument");
   if (q->n_mom < 2) return fail(TBK_ERR_INVALID, "n must be greater than or equal to 2");
   if (q->R < 1) return fail(TBK_ERR_INVALID, "R must be >= 1");
-  if (q->precision != TBK_PREC_MIXED && q->precision != TBK_PREC_FP64)
+  if (q->precision != TBK_PREC_MIXED && q->precision != TBK_PREC_FP64 && q->precision != TBK_PREC_DD)
     return fail(TBK_ERR_INVALID, "unknown precision %d", q->precision);
   if (q->build_mode < 0 || q->build_mode > 2) return fail(TBK_ERR_INVALID, "unknown build mode %d", q->build_mode);
   if (!(q->e_max > q->e_min)) return fail(TBK_ERR_INVALID, "spectral bounds need e_max > e_min");
@@ -407,7 +408,9 @@ Footprint footprint_of(const tbk_request& q, const tbk_lattice_s& L) {
   if (!L.removed.empty()) fields += 9 * N;
   const int64_t build = csc(nnz) + fields;
   const int64_t rescale = csc(nnz) + csc(nnz + N) + 8 * (N + 1);
-  const int64_t ell_all = 8 * (NS + 1) + (E + 32) * (4 + 12 * vs) + Np * 12 * vs;
+  // FP64 and FP32 values, plus the double-float copy for double-float requests
+  const int64_t vals = q.precision == TBK_PREC_DD ? 20 : 12;
+  const int64_t ell_all = 8 * (NS + 1) + (E + 32) * (4 + vals * vs) + Np * vals * vs;
   const int64_t ell = csc(nnz + N) + 12 * (N + 1) + 12 * (nnz + N + 1) + ell_all;
   const int64_t ell_keep = 4 * (NS + 1) + (E + 32) * (4 + hs * vs) + Np * hs * vs;
   const int rc = width_for(q.precision, q.R);
@@ -512,7 +515,7 @@ struct tbk_server_s {
   char* stage[2] = {nullptr, nullptr};
   cudaEvent_t copy_ev[2] = {nullptr, nullptr};
   bool copy_pending[2] = {false, false};
-  std::unordered_map<uint64_t, cudaGraphExec_t> graphs;   // key: group mask | round length << 32
+  std::map<std::pair<uint64_t, int>, cudaGraphExec_t> graphs;   // key: (group mask, round length)
   // launch shapes per group code
   int grid[kGroups] = {};
   int pf[kGroups] = {};
@@ -520,6 +523,9 @@ struct tbk_server_s {
   bool tuned[kGroups] = {};
   // requests
   std::mutex mu;
+  // graph capture and device builds never overlap: a build's first launch of a
+  // kernel may load its module, which CUDA refuses while any stream captures
+  std::mutex capture_mu;
   std::condition_variable cv_admit, cv_loop, cv_done;
   std::deque<SrvRequest*> queued, ready;
   std::unordered_map<int64_t, std::unique_ptr<SrvRequest>> all;
@@ -583,8 +589,9 @@ int build_request(tbk_server_s* S, SrvRequest* r) {
   Ht->row_idx.release();
   Ht->values.release();
   const bool mixed = q.precision == TBK_PREC_MIXED;
-  if (mixed) { Ht->ell.val64.release(); Ht->ell.diag64.release(); }
-  else { Ht->ell.val32.release(); Ht->ell.diag32.release(); }
+  if (q.precision == TBK_PREC_DD) TBK_TRY(ensure_ell_dd(Ht, st));
+  if (q.precision != TBK_PREC_FP64) { Ht->ell.val64.release(); Ht->ell.diag64.release(); }
+  if (!mixed) { Ht->ell.val32.release(); Ht->ell.diag32.release(); }
   r->n = Ht->rows;
   r->rc = width_for(q.precision, q.R);
   r->cs = mixed ? 8 : 16;
@@ -648,7 +655,11 @@ void admit_main(tbk_server_s* S) {
       r->state = ST_BUILDING;
       r->t_build0 = S->now_ms();
     }
-    const int s = S->broken ? TBK_ERR_CUDA : build_request(S, r);
+    int s;
+    {
+      std::lock_guard<std::mutex> cap(S->capture_mu);
+      s = S->broken ? TBK_ERR_CUDA : build_request(S, r);
+    }
     const std::string msg = s == TBK_OK ? std::string() : std::string(tbk_last_error());
     {
       std::lock_guard<std::mutex> lk(S->mu);
@@ -696,10 +707,11 @@ int ensure_tables(tbk_server_s* S, int32_t lanes, int32_t slabs, int32_t reqs) {
   return TBK_OK;
 }
 
-int capture_graph(tbk_server_s* S, uint32_t mask, int steps, cudaGraphExec_t* out) {
-  const uint64_t key = (uint64_t)mask | ((uint64_t)steps << 32);
+int capture_graph(tbk_server_s* S, uint64_t mask, int steps, cudaGraphExec_t* out) {
+  const std::pair<uint64_t, int> key(mask, steps);
   auto it = S->graphs.find(key);
   if (it != S->graphs.end()) { *out = it->second; return TBK_OK; }
+  std::lock_guard<std::mutex> cap(S->capture_mu);
   cudaStream_t st = S->st_loop;
   const char* base = S->dtab.as<char>();
   LaunchArgs a;
@@ -712,7 +724,7 @@ int capture_graph(tbk_server_s* S, uint32_t mask, int steps, cudaGraphExec_t* ou
   int rc = TBK_OK;
   cudaError_t e = cudaEventRecord(S->ev_fork, st);
   for (int code = 0; code < kGroups && e == cudaSuccess && rc == TBK_OK; ++code) {
-    if (!(mask & (1u << code))) continue;
+    if (!(mask & (1ull << code))) continue;
     const GroupFns fn = group_fns(code);
     if (!fn.launch) { rc = fail(TBK_ERR_UNSUPPORTED, "group %d not instantiated", code); break; }
     cudaStream_t sd = S->side[code];
@@ -808,12 +820,12 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
   SReq* reqs = reinterpret_cast<SReq*>(hb + S->off_reqs);
   memset(hdr, 0, sizeof(SHdr));
   Round rd;
-  uint32_t mask = 0;
+  uint64_t mask = 0;
   int32_t li = 0, si = 0;
   for (int32_t qi = 0; qi < n_reqs; ++qi) {
     SrvRequest* r = order[qi];
     const int code = r->code;
-    if (!(mask & (1u << code))) { mask |= 1u << code; hdr->grp_begin[code] = si; }
+    if (!(mask & (1ull << code))) { mask |= 1ull << code; hdr->grp_begin[code] = si; }
     const int32_t sr = r->slab_rows;
     const int32_t steps = std::min(RS, r->n_steps - r->s0);
     SReq& q = reqs[qi];
@@ -826,13 +838,13 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
     q.n_mom = r->q.n_mom;
     q.finishing = r->s0 + RS >= r->n_steps ? 1 : 0;
     const EllDev& E = r->Ht->ell;
-    const bool mixed = r->q.precision == TBK_PREC_MIXED;
     for (int32_t c = 0; c < r->n_lanes; ++c) {
       SLane& L = lanes[li];
       L.soff = E.slice_off.as<int32_t>();
       L.ecol = E.col.as<int32_t>();
-      L.eval = mixed ? E.val32.p : E.val64.p;
-      L.diag = mixed ? E.diag32.p : E.diag64.p;
+      const int pq = r->q.precision;
+      L.eval = pq == TBK_PREC_MIXED ? E.val32.p : pq == TBK_PREC_DD ? E.valdd.p : E.val64.p;
+      L.diag = pq == TBK_PREC_MIXED ? E.diag32.p : pq == TBK_PREC_DD ? E.diagdd.p : E.diag64.p;
       L.va = r->vec[2 * c].p;
       L.vb = r->vec[2 * c + 1].p;
       L.n = r->n;
@@ -876,7 +888,7 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
   TBK_CUDA(cudaGraphLaunch(gx, st));
   TBK_CUDA(cudaEventRecord(rd.ev1, st));
   int groups = 0;
-  for (int c = 0; c < kGroups; ++c) groups += (mask >> c) & 1;
+  for (int c = 0; c < kGroups; ++c) groups += (int)((mask >> c) & 1);
   rd.launches = (int64_t)groups * RS + 2;
   // advance: who is left for the next round
   std::vector<SrvRequest*> next;
@@ -958,7 +970,7 @@ int autotune(tbk_server_s* S) {
   TBK_CUDA(cudaEventCreate(&e0));
   TBK_CUDA(cudaEventCreate(&e1));
   int rc_all = TBK_OK;
-  for (int prec = 0; prec < 2 && rc_all == TBK_OK; ++prec) {
+  for (int prec = 0; prec < 3 && rc_all == TBK_OK; ++prec) {
     for (int rc = 4; rc <= (prec == TBK_PREC_MIXED ? 64 : 32); rc <<= 1) {
       const int code = group_code(prec, rc, false);
       const GroupFns fn = group_fns(code);
@@ -981,6 +993,10 @@ int autotune(tbk_server_s* S) {
         srv_synth_ell_kernel<float><<<(ns * 32 + T) / T, T, 0, st>>>(n, ns, soff.as<int32_t>(), ecol.as<int32_t>(),
                                                                     eval.as<float>(), diag.as<float>());
       else
+        if (prec == TBK_PREC_DD)
+          srv_synth_ell_kernel<dd><<<(ns * 32 + T) / T, T, 0, st>>>(n, ns, soff.as<int32_t>(), ecol.as<int32_t>(),
+                                                                   eval.as<dd>(), diag.as<dd>());
+        else
         srv_synth_ell_kernel<double><<<(ns * 32 + T) / T, T, 0, st>>>(n, ns, soff.as<int32_t>(), ecol.as<int32_t>(),
                                                                      eval.as<double>(), diag.as<double>());
       TBK_CUDA(cudaGetLastError());

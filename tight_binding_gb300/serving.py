@@ -46,7 +46,7 @@ def model_bounds(kind: str, W: float, t: float = 1.0, margin: float = 0.05) -> t
     return -e, e
 
 
-PRECISION = {"mixed": capi.PREC_MIXED, "fp64": capi.PREC_FP64}
+PRECISION = {"mixed": capi.PREC_MIXED, "fp64": capi.PREC_FP64, "dd": capi.PREC_DD}
 MODES = {"periodic": capi.BUILD_PERIODIC_BARE, "open": capi.BUILD_SPARSE, "bare": capi.BUILD_BARE}
 STATS_KEYS = ("done", "failed", "rounds", "graphs", "busy_ms", "bytes", "updates", "launches", "budget_bytes",
               "peak_reserved_bytes", "reserved_bytes", "build_ms", "peak_resident", "build_overshoot_bytes")
