@@ -40,9 +40,6 @@
 namespace tbk {
 namespace {
 
-#ifndef TBK_SERVE_MIN_BLOCKS
-#define TBK_SERVE_MIN_BLOCKS 4      // resident CTAs per SM the step kernel is compiled for
-#endif
 constexpr int kSrvThreads = 256;
 constexpr int kSrvWarps = kSrvThreads / 32;
 constexpr int kIterPerSlab = 8;        // warp iterations (512 B of v_s each) per slab
@@ -81,7 +78,10 @@ __host__ __device__ constexpr int srv_rows_per_warp(int cs, int R) { return 32 /
 inline int srv_slab_rows(int cs, int R, int64_t) { return srv_rows_per_warp(cs, R) * kIterPerSlab; }
 
 // One doubling recursion step (step j of the round) over the slabs of group g,
-// one warp per slab (no barriers: warps run independently).  With s = s0 + j
+// one warp per slab (no barriers: warps run independently).  The six pointers
+// of the slab's lane live in a per-warp shared-memory slot read at each use, so
+// that they hold no registers across the gathers: complex64 groups fit 5 CTAs
+// per SM (wider types keep 4).  With s = s0 + j
 // the lane's step, x = v_s and y = v_{s-1} on entry:
 //   s == 0:         y = H x,             partials <x|x>, <x|y>
 //   0 < s < last:   y = 2 H x - y,       partials <x|x>, <x|y_in>
@@ -89,7 +89,7 @@ inline int srv_slab_rows(int cs, int R, int64_t) { return srv_rows_per_warp(cs, 
 // which are the step sums of the doubling identities mu_2s = 2<v_s|v_s> - mu_0,
 // mu_2s-1 = 2<v_s|v_s-1> - mu_1.
 template <typename F, int R, bool CPLX_H>
-__global__ void __launch_bounds__(kSrvThreads, TBK_SERVE_MIN_BLOCKS) srv_step_kernel(
+__global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_kernel(
     const SHdr* __restrict__ hdr, const SLane* __restrict__ lanes, const SSlab* __restrict__ slabs, int32_t g,
     int32_t j, int32_t reverse, int32_t pf_dist, double* __restrict__ part, int32_t slab_cap) {
   using CT = typename C2<F>::T;
@@ -103,35 +103,15 @@ __global__ void __launch_bounds__(kSrvThreads, TBK_SERVE_MIN_BLOCKS) srv_step_ke
   const int sub = lane % LPR;
   const int32_t begin = hdr->grp_begin[g], cnt = hdr->grp_count[g];
   const int32_t nw = (int32_t)gridDim.x * kSrvWarps;
-  int32_t t = (int32_t)blockIdx.x * kSrvWarps + (threadIdx.x >> 5);
-  SSlab nxt = t < cnt ? slabs[begin + (reverse ? cnt - 1 - t : t)] : SSlab{-1, 0};
-  // fields of the lane last seen (consecutive slabs of a warp mostly share it)
-  int32_t cl = -1, n = 0, ns = 0, s = 0, slab_rows = 0;
-  const CT* xa = nullptr;
-  CT* ya = nullptr;
-  const int32_t* soff = nullptr;
-  const int32_t* ecol = nullptr;
-  const F* eval = nullptr;
-  const F* diag = nullptr;
-  for (; t < cnt; t += nw) {
+  struct WP { const CT* x; CT* y; const int32_t* soff; const int32_t* ecol; const F* eval; const F* diag; };
+  __shared__ WP wp[kSrvWarps];
+  volatile WP* my = wp + (threadIdx.x >> 5);
+  for (int32_t t = (int32_t)blockIdx.x * kSrvWarps + (threadIdx.x >> 5); t < cnt; t += nw) {
     const int32_t i = reverse ? cnt - 1 - t : t;
-    const SSlab sl = nxt;
-    if (t + nw < cnt) nxt = slabs[begin + (reverse ? cnt - 1 - (t + nw) : t + nw)];   // in flight meanwhile
-    if (sl.lane != cl) {
-      const SLane* L = lanes + sl.lane;
-      cl = sl.lane;
-      n = L->n;
-      ns = L->n_steps;
-      s = L->s0 + j;
-      slab_rows = L->slab_rows;
-      xa = static_cast<const CT*>((s & 1) ? L->vb : L->va);
-      ya = static_cast<CT*>((s & 1) ? L->va : L->vb);
-      soff = L->soff;
-      ecol = L->ecol;
-      eval = static_cast<const F*>(L->eval);
-      diag = static_cast<const F*>(L->diag);
-    }
-    if (s >= ns) continue;                       // uniform over the warp
+    const SSlab sl = slabs[begin + i];
+    const SLane* L = lanes + sl.lane;
+    const int32_t n = L->n, ns = L->n_steps, s = L->s0 + j, slab_rows = L->slab_rows;
+    if (s >= ns) continue;
     if (pf_dist > 0 && lane == 0) {
       // the slab this warp reaches pf_dist iterations later: v_s, v_{s-1} rows into L2
       const int32_t tf = t + pf_dist * nw;
@@ -151,20 +131,27 @@ __global__ void __launch_bounds__(kSrvThreads, TBK_SERVE_MIN_BLOCKS) srv_step_ke
         }
       }
     }
+    if (lane == 0) {
+      my->x = static_cast<const CT*>((s & 1) ? L->vb : L->va);
+      my->y = static_cast<CT*>((s & 1) ? L->va : L->vb);
+      my->soff = L->soff;
+      my->ecol = L->ecol;
+      my->eval = static_cast<const F*>(L->eval);
+      my->diag = static_cast<const F*>(L->diag);
+    }
+    __syncwarp();
     const bool first = s == 0;
     const bool dot_only = s == ns - 1 && s > 0;
-    const CT* x = xa;
-    CT* y = ya;
     const int32_t rend = min(sl.row0 + slab_rows, n);
     F m0 = 0, m1 = 0;
     for (int32_t rb = sl.row0; rb < rend; rb += RPW) {
       const int32_t r = rb + lane / LPR;
       if (r >= rend) break;
       const int64_t me = (int64_t)r * LPR + sub;
-      const LaneV<F, VPL> xs = ld_ro<F, VPL>(x + me * VPL);
+      const LaneV<F, VPL> xs = ld_ro<F, VPL>(my->x + me * VPL);
       LaneV<F, VPL> prev;
       if (!first) {
-        prev = ld_stream<F, VPL>(y + me * VPL);
+        prev = ld_stream<F, VPL>(my->y + me * VPL);
       } else {
 #pragma unroll
         for (int q = 0; q < VPL; ++q) { prev.re[q] = 0; prev.im[q] = 0; }
@@ -173,23 +160,26 @@ __global__ void __launch_bounds__(kSrvThreads, TBK_SERVE_MIN_BLOCKS) srv_step_ke
 #pragma unroll
       for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
       if (!dot_only) {
-        HVal<F, CPLX_H>::load(diag, r).template fma<VPL>(xs, acc);
+        HVal<F, CPLX_H>::load(my->diag, r).template fma<VPL>(xs, acc);
         const int32_t sidx = r >> 5, l = r & 31;
-        const int32_t off = soff[sidx];
-        const int32_t w = (soff[sidx + 1] - off) >> 5;
-        const int32_t* cp = ecol + off + l;
+        const int32_t* so = my->soff;
+        const int32_t off = so[sidx];
+        const int32_t w = (so[sidx + 1] - off) >> 5;
         for (int k = 0; k < w; k += 4) {
+          const int32_t* cp = my->ecol + off + l;
+          const F* ev = my->eval;
           int32_t c[4];
           HVal<F, CPLX_H> h[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
             const bool v = k + u < w;
             c[u] = v ? __ldg(cp + (k + u) * 32) : r;
-            h[u] = v ? HVal<F, CPLX_H>::load(eval, off + l + (int64_t)(k + u) * 32) : HVal<F, CPLX_H>::zero();
+            h[u] = v ? HVal<F, CPLX_H>::load(ev, off + l + (int64_t)(k + u) * 32) : HVal<F, CPLX_H>::zero();
           }
+          const CT* xp = my->x;
           LaneV<F, VPL> xv[4];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) xv[u] = ld_ro<F, VPL>(x + ((int64_t)c[u] * LPR + sub) * VPL);
+          for (int u = 0; u < 4; ++u) xv[u] = ld_ro<F, VPL>(xp + ((int64_t)c[u] * LPR + sub) * VPL);
 #pragma unroll
           for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
         }
@@ -206,8 +196,9 @@ __global__ void __launch_bounds__(kSrvThreads, TBK_SERVE_MIN_BLOCKS) srv_step_ke
         if (first) m1 += xs.re[q] * out.re[q] + xs.im[q] * out.im[q];
         else m1 += xs.re[q] * prev.re[q] + xs.im[q] * prev.im[q];
       }
-      if (!dot_only) st_v<F, VPL>(y + me * VPL, out);
+      if (!dot_only) st_v<F, VPL>(my->y + me * VPL, out);
     }
+    __syncwarp();
     // slab partial in FP64: a fixed shuffle tree, lane 0 writes
     double d0 = (double)m0, d1 = (double)m1;
 #pragma unroll
@@ -1168,7 +1159,7 @@ int tbk_server_create(tbk_server* out, const tbk_server_config* cfg) {
   for (int code = 0; code < kGroups; ++code) {
     const GroupFns fn = group_fns(code);
     S->grid[code] = fn.occ ? fn.occ() * S->sms : S->sms;
-    S->pf[code] = 1;
+    S->pf[code] = 0;                     // untuned: no L2 prefetch (the tuner may pick one)
   }
   if (cfg && cfg->autotune) {
     const int s = autotune(S);
