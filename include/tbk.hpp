@@ -7,6 +7,7 @@
 //   cuda::Cheb_first_kind_seq_braket   TB/numerics_cuda.cuh:10-13
 //   bases_of_uniform_ampl_with_random_phases  TB/numerical.h:120-122 (seeded)
 //   density_of_states_seq              TB/functions.h:15-32
+//   DosServer                          (no counterpart: many solves advanced together)
 // Sparse matrices live on the device (SparseMatrix owns a tbk_sparse); dense
 // blocks use the Eigen::MatrixXcd layout (column-major complex128).  Failures
 // throw std::runtime_error carrying tbk_last_error(); the reference's
@@ -15,6 +16,7 @@
 #include <array>
 #include <complex>
 #include <cstdint>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -299,5 +301,53 @@ std::vector<double> density_of_states_seq(PartialLattice<Dim>& X, int N, const s
   for (double e : E_list) dos.push_back(-1.0 / R / 3.14159265358979323846 * f(e));
   return dos;
 }
+
+// Many DoS solves advanced together (tbk_server_*): submit lattices, poll moments.
+class DosServer {
+ public:
+  explicit DosServer(double budget_gb = 120.0, int steps_per_round = 16, bool autotune = true,
+                     int max_resident = 4096, int result_arena_mb = 64, double step_gb = 2.0) {
+    tbk_server_config cfg{budget_gb, steps_per_round, autotune ? 1 : 0, max_resident, result_arena_mb, step_gb};
+    check(tbk_server_create(&h_, &cfg));
+  }
+  DosServer(const DosServer&) = delete;
+  DosServer& operator=(const DosServer&) = delete;
+  ~DosServer() { tbk_server_destroy(h_); }
+
+  // periodic bare Hamiltonian of X (every axis periodic), bounds [e_min, e_max]
+  template <int Dim>
+  int64_t submit(const PartialLattice<Dim>& X, int n_mom, int R, uint64_t seed, double e_min, double e_max,
+                 int precision = TBK_PREC_MIXED) {
+    tbk_request q{};
+    q.lattice = X.handle();
+    q.build_mode = TBK_BUILD_PERIODIC_BARE;
+    for (int i = 0; i < 3; ++i) q.extend[i] = i < Dim ? 1 : 0;
+    q.is_complex = 0;
+    q.n_mom = n_mom;
+    q.R = R;
+    q.precision = precision;
+    q.seed = seed;
+    q.e_min = e_min;
+    q.e_max = e_max;
+    int64_t t = 0;
+    check(tbk_server_submit(h_, &q, &t));
+    n_mom_[t] = n_mom;
+    return t;
+  }
+  // true and the moments when done within wait_ms; throws if the request failed
+  bool poll(int64_t ticket, int wait_ms, std::vector<double>& mu, double times_ms[4] = nullptr) {
+    mu.resize((size_t)n_mom_.at(ticket));
+    const int s = tbk_server_poll(h_, ticket, wait_ms, mu.data(), times_ms);
+    if (s == TBK_PENDING) return false;
+    n_mom_.erase(ticket);
+    check(s);
+    return true;
+  }
+  tbk_server handle() const { return h_; }
+
+ private:
+  tbk_server h_ = nullptr;
+  std::map<int64_t, int> n_mom_;
+};
 
 }  // namespace tbk

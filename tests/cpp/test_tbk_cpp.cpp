@@ -9,6 +9,8 @@
 //      the grid, integrates to ~1 (trapezoid), matches the DCT-III route
 //   4. bras != kets (plain braket) equals bras == kets (doubling) on the same
 //      kets to 1e-12
+//   5. DosServer: a double-float request equals the FP64 solve to 1e-10, and
+//      the same request twice gives the same bits
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -117,6 +119,33 @@ int main() {
     double err = 0.0;
     for (int n = 0; n < 100; ++n) err = std::fmax(err, std::fabs(mu_d[n] - mu_p[n]) / mu_p[0]);
     expect(err < 1e-12, "doubling equals the plain braket (FP64)", err);
+  }
+  // ---- 5. the serving API: a request through the server equals the same
+  //         request alone (moments of the same seeded kets)
+  {
+    UnitCell<2> square({{1, 0, 0}, {0, 1, 0}}, {{"A", {0, 0, 0}}});
+    square.add_hopping("A", 1, Complex(1.0, 0.0));
+    PartialLattice<2> X(square, {40, 40});
+    X.set_scalar_disorder(0.6, 4);
+    DosServer srv(4.0, 8, false);
+    const int64_t a = srv.submit(X, 96, 8, 11, -4.4, 4.4, TBK_PREC_DD);
+    const int64_t b = srv.submit(X, 96, 8, 11, -4.4, 4.4, TBK_PREC_DD);
+    std::vector<double> ma, mb;
+    int tries = 0;
+    while (!srv.poll(a, 100, ma) && ++tries < 600) {}
+    tries = 0;
+    while (!srv.poll(b, 100, mb) && ++tries < 600) {}
+    SparseMatrix H = X.get_Hamiltonian_periodic_extend_bare_sparse<double>({1, 1});
+    GreenFunction G(96, H, -4.4, 4.4);
+    MatrixXcd kets = bases_of_uniform_ampl_with_random_phases(X.get_total_number(), 8, 11);
+    auto ref = cuda::Cheb_first_kind_seq_braket(G.scaled_HE, 96, kets, kets, TBK_PREC_FP64);
+    double err = 0.0, same = 0.0;
+    for (int n = 0; n < 96 && ma.size() == 96 && mb.size() == 96; ++n) {
+      err = std::fmax(err, std::fabs(ma[n] - ref[n]) / ref[0]);
+      same = std::fmax(same, std::fabs(ma[n] - mb[n]));
+    }
+    expect(ma.size() == 96 && err <= 1e-10, "server (double-float) equals the FP64 solve", err);
+    expect(same == 0.0, "the same request twice gives the same bits", same);
   }
   std::printf("%s\n", failures ? "FAILED" : "ALL PASSED");
   return failures ? 1 : 0;

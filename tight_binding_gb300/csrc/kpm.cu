@@ -48,7 +48,8 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     int32_t n, int32_t n_tiles, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
     const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
     typename C2<F>::T* y, const typename C2<F>::T* pv, const typename C2<F>::T* __restrict__ bras,
-    double* __restrict__ part, int store, int reverse, int gather, int pf_dist) {
+    double* __restrict__ part, int store, int reverse, int gather, int pf_dist, float2* __restrict__ kstore,
+    int32_t kM, int32_t km) {
   using CT = typename C2<F>::T;
   constexpr int VPL = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
   constexpr int LPR = R / VPL;             // lanes per row
@@ -136,6 +137,15 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
       }
     }
     if (store) st_v<F, VPL>(y + me * VPL, out);
+    if (kstore) {
+      // block km of a complex64 K-tiled store (element k of block m at
+      // ((k/16)*kM + m)*16 + k%16, k = row * R + vector): one rounding per value
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) {
+        const int64_t k = (int64_t)r * R + sub * VPL + q;
+        kstore[((k >> 4) * kM + km) * 16 + (k & 15)] = make_float2(to_f32(out.re[q]), to_f32(out.im[q]));
+      }
+    }
   }
   // FP64 from here on: warp shuffle, then across the CTA's warps
   double d0 = (double)m0, d1 = (double)m1;
@@ -263,6 +273,8 @@ struct StepArgs {
   const void* bras;
   double* part;
   int store, reverse, gather, pf_dist;
+  float2* kstore = nullptr;   // optional complex64 K-tiled copy of the output (Kubo blocks)
+  int32_t kM = 0, km = 0;
 };
 
 template <typename F, int R, bool CPLX_H>
@@ -276,7 +288,8 @@ static int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
   auto dg = static_cast<const F*>(a.diag);
 #define TBK_STEP(FI, BR)                                                                   \
   kpm_step_kernel<F, R, CPLX_H, FI, BR><<<grid, kStepThreads, 0, st>>>(                    \
-      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist)
+      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.kstore, \
+      a.kM, a.km)
   if (first) { if (braket) TBK_STEP(true, true); else TBK_STEP(true, false); }
   else { if (braket) TBK_STEP(false, true); else TBK_STEP(false, false); }
 #undef TBK_STEP
@@ -407,7 +420,7 @@ int step_config(tbk_sparse_s* A, int Rc, int prec, int* grid, int* n_tiles, cuda
 }
 
 int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
-             int grid, int n_tiles, cudaStream_t st) {
+             int grid, int n_tiles, cudaStream_t st, float2* kstore, int32_t kM, int32_t km, bool store_y) {
   StepArgs a;
   a.n = A->rows;
   a.n_tiles = n_tiles;
@@ -422,10 +435,13 @@ int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const vo
   a.pv = first ? y : pv;
   a.bras = nullptr;
   a.part = part;
-  a.store = 1;
+  a.store = store_y ? 1 : 0;
   a.reverse = 0;
   a.gather = 1;
   a.pf_dist = 1;
+  a.kstore = kstore;
+  a.kM = kM;
+  a.km = km;
   const bool c = A->ell.cplx != 0;
   if (prec == TBK_PREC_FP64)
     return c ? launch_step<double, true>(Rc, a, first, false, grid, st) : launch_step<double, false>(Rc, a, first, false, grid, st);

@@ -49,6 +49,10 @@ __device__ __forceinline__ dd& operator+=(dd& a, dd b) { a = a + b; return a; }
 struct __align__(16) dd2 {
   dd x, y;
 };
+// round to FP32 once
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(double v) { return __double2float_rn(v); }
+__device__ __forceinline__ float to_f32(dd v) { return __fadd_rn(v.hi, v.lo); }
 
 template <typename F> struct C2;
 template <> struct C2<float> { using T = float2; };

@@ -292,7 +292,14 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     TBK_CHECK_LAUNCH();
     return TBK_OK;
   };
-  // one side: store[m] = Aout T_m(H~) (Bin v0), m < M
+  // block m of `store` = A x, written by the product itself (no work block)
+  auto apply_to_store = [&](tbk_sparse_s* A, const void* x, void* scratch, float2* store, int32_t m) -> int {
+    int g, t;
+    TBK_TRY(step_config(A, Rc, prec, &g, &t, st));
+    return step_any(A, Rc, prec, x, scratch, nullptr, true, partd.as<double>(), g, t, st, store, M, m, false);
+  };
+  // one side: store[m] = Aout T_m(H~) (Bin v0), m < M; each step writes its
+  // complex64 block (Aout absent) or feeds the product that does
   auto side = [&](tbk_sparse_s* Aout, tbk_sparse_s* Bin, float2* store) -> int {
     void* r[3] = {wblk(0), wblk(1), wblk(2)};
     void* tmpA = wblk(3);
@@ -303,10 +310,11 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
       if (m >= 1) {
         const void* x = r[(m - 1) % 3];
         const void* pv = m >= 2 ? r[(m - 2) % 3] : nullptr;
-        TBK_TRY(step_any(Ht, Rc, prec, x, y, pv, m == 1, partd.as<double>(), grid, n_tiles, st));
+        TBK_TRY(step_any(Ht, Rc, prec, x, y, pv, m == 1, partd.as<double>(), grid, n_tiles, st,
+                         Aout ? nullptr : store, M, m, true));
       }
-      if (Aout) { TBK_TRY(apply(Aout, y, tmpA)); TBK_TRY(round_to(tmpA, store, m)); }
-      else TBK_TRY(round_to(y, store, m));
+      if (Aout) TBK_TRY(apply_to_store(Aout, y, tmpA, store, m));
+      else if (m == 0) TBK_TRY(round_to(y, store, 0));
     }
     return TBK_OK;
   };

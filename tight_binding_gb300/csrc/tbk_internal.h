@@ -128,8 +128,11 @@ int sm_count();
 // or y = 2 H x - pv; moment partials into part[2 * grid].  Block loaders:
 // Eigen-layout kets / seeded random phases.
 int step_config(tbk_sparse_s* A, int Rc, int prec, int* grid, int* n_tiles, cudaStream_t st);
+// kstore: optional complex64 K-tiled store that receives the step's output as
+// block km of kM (store_y false: only there)
 int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
-             int grid, int n_tiles, cudaStream_t st);
+             int grid, int n_tiles, cudaStream_t st, float2* kstore = nullptr, int32_t kM = 0, int32_t km = 0,
+             bool store_y = true);
 int load_block_any(int prec, int32_t n, int32_t R, int32_t r0, int32_t Rp, const double2* src, void* dst,
                    cudaStream_t st);
 int random_block_any(int prec, int32_t n, int32_t R, int32_t r0, int32_t Rp, uint64_t seed, void* dst,
