@@ -120,8 +120,22 @@ int tbk_lattice_set_scalar_sites(tbk_lattice lat, const double* V_sites);
 /* set_scalar_field with Anderson disorder V = W (u - 1/2), u ~ U[0,1) keyed by
  * (seed, bare site index); generated on the device. */
 int tbk_lattice_set_scalar_disorder(tbk_lattice lat, double W, uint64_t seed);
-/* remove_atoms(atom, cells), TB/lattice.h:389-402: bare site flags (N, 1 = removed). */
+/* Vacancies (TB/lattice.h:389-464).  Removed sites drop out of the open-boundary
+ * Hamiltonian (get_Hamiltonian_sparse) and the position operators; the bare ->
+ * compressed index (index_comp_construct) is a device prefix-sum compaction at
+ * build time.  set_removed: bare site flags (N, 1 = removed; NULL clears). */
 int tbk_lattice_set_removed(tbk_lattice lat, const uint8_t* removed_sites);
+/* remove_atoms(atom_name, cells), TB/lattice.h:389-402: `n` lattice vectors
+ * (n x Dim int32, row-major); the atom `atom` of each cell is removed.  Unknown
+ * atom: TBK_ERR_INVALID "Atom <name> does not exist in the unit cell." */
+int tbk_lattice_remove_atoms(tbk_lattice lat, const char* atom, const int32_t* cells, int64_t n);
+/* remove_atoms_random(atom_name, n), TB/lattice.h:404-418: `n` distinct cells
+ * drawn from a seeded stream (the reference seeds from std::random_device);
+ * n > cell number: TBK_ERR_INVALID "The random selection is larger than the
+ * total number." */
+int tbk_lattice_remove_atoms_random(tbk_lattice lat, const char* atom, int64_t n, uint64_t seed);
+/* The current removal flags (N bytes, 1 = removed). */
+int tbk_lattice_get_removed(tbk_lattice lat, uint8_t* removed_sites);
 /* index_comp construction, TB/lattice.h:446-457: number of kept sites. */
 int tbk_lattice_kept_number(tbk_lattice lat, int64_t* n);
 
@@ -156,6 +170,70 @@ int tbk_sparse_rescale(tbk_sparse* out, tbk_sparse H, double a, double b, void* 
 /* Velocity: v = X H - H X with X = op_position(axis) (values x_i h - h x_j,
  * same pattern as H), TB/lattice.h:338-345 and TB/snippets.h:316-317. */
 int tbk_sparse_commutator(tbk_sparse* out, tbk_sparse H, tbk_sparse X, void* stream);
+/* Extreme eigenvalues of a Hermitian matrix by `iters` Lanczos steps on the
+ * device from seeded random phases (the reference's matrix_spectral_range_sparse,
+ * TB/numerical.h:24-46, which uses Spectra on the CPU and refuses > 5,000
+ * rows): the extreme Ritz values e_min, e_max and their residual norms
+ * (res_min / res_max may be NULL; an eigenvalue lies within that distance). */
+int tbk_spectral_range(tbk_sparse A, int32_t iters, uint64_t seed, double* e_min, double* e_max,
+                       double* res_min, double* res_max, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Chebyshev expansions applied to vectors
+ * ------------------------------------------------------------------------ */
+/* out = sum_{k < n_terms} coef_k T_k(H~) kets for R column-major complex128
+ * vectors (host, n x R; coef complex, interleaved re/im).  Replaces walking
+ * Cheb_first_kind_seq_view (TB/numerical.h:346-361) and summing on the host, as
+ * conductivity_test_sawtooth does (TB/snippets.h:173-223).  precision:
+ * TBK_PREC_FP64 / TBK_PREC_DD / TBK_PREC_MIXED for the recursion; the sum is
+ * accumulated in complex128. */
+int tbk_cheb_expand(tbk_sparse Ht, int32_t n_terms, const double* coef, int32_t R, const double* kets, double* out,
+                    int32_t precision, void* stream);
+/* Delta-projection coefficients of conductivity_test_sawtooth (TB/snippets.h:
+ * 175, 194-202): coef_k = a_d(k) T_k(e), a_d(0) = 1, a_d(k>0) = 2, for
+ * k = 0 .. N (N + 1 complex values). */
+int tbk_cheb_coef_delta(double e, int32_t N, double* coef);
+/* exp(-i H t) for H = a H~ + b: coef_k = exp(-i b t) (2 - delta_k0) (-i)^k J_k(a t). */
+int tbk_cheb_coef_evolution(double a, double b, double t, int32_t n_terms, double* coef);
+/* Number of terms after which |J_k(a t)| stays below tol. */
+int tbk_cheb_evolution_terms(double a, double t, double tol, int32_t* n_terms);
+
+/* ---------------------------------------------------------------------------
+ * Moment files: binary replacement of the text dumps of utils::output_to_file
+ * (TB/utils.h:42-69) and generate_V_moments' V_moments.txt (TB/snippets.h:
+ * 504-517).  One file = a fixed 256-byte little-endian header, then rows x cols
+ * values (doubles; complex: interleaved re/im) in row-major order.  The header
+ * carries what is needed to reuse the moments (bounds, R, seed, kernel,
+ * precision) and an FNV-1a 64 checksum of the data bytes, checked on load.
+ * ------------------------------------------------------------------------ */
+enum {
+  TBK_MOMENTS_DOS = 1,      /* mu_n, n < rows (cols = 1), real                 */
+  TBK_MOMENTS_MU_NM = 2,    /* mu_nm (rows x cols), complex (Kubo)             */
+  TBK_MOMENTS_V_NM = 3      /* V_nm, upper triangle (rows x cols), real        */
+};
+typedef struct tbk_moments_header {
+  char magic[8];            /* "TBKMOM" 0 1                                   */
+  int32_t version;          /* 1                                               */
+  int32_t kind;             /* TBK_MOMENTS_*                                   */
+  int32_t rows, cols;
+  int32_t is_complex;
+  int32_t R;                /* random vectors summed                           */
+  int32_t precision;        /* TBK_PREC_* of the recursion                     */
+  int32_t kernel;           /* TBK_KERNEL_* applied, -1 = raw moments         */
+  uint64_t seed;
+  double e_min, e_max;      /* spectral bounds of H~ = (H - b)/a               */
+  double kernel_p0, kernel_p1;
+  int64_t n_sites;
+  uint64_t checksum;        /* FNV-1a 64 of the data bytes (written by save)   */
+  char label[160];          /* free text (model, lattice), NUL-terminated      */
+} tbk_moments_header;
+/* Writes header + data (the magic, version and checksum are filled in). */
+int tbk_moments_save(const char* path, const tbk_moments_header* header, const double* data);
+/* Reads the header only. */
+int tbk_moments_load_header(const char* path, tbk_moments_header* header);
+/* Reads header and data; capacity in doubles.  TBK_ERR_INVALID on a bad magic,
+ * a short file, too small a buffer or a checksum mismatch. */
+int tbk_moments_load(const char* path, tbk_moments_header* header, double* data, int64_t capacity);
 
 /* =========================================================================
  * Chebyshev (KPM) moments.

@@ -4,6 +4,8 @@
 //   UnitCell<Dim>                      TB/unit_cell.h:65-156
 //   PartialLattice<Dim>                TB/lattice.h:22-103
 //   GreenFunction / GreenFunctionImag  TB/lattice.h:545-647
+//   matrix_spectral_range_sparse       TB/numerical.h:24-46 (device Lanczos)
+//   cheb_expand / time_evolve          TB/numerical.h:346-361
 //   cuda::Cheb_first_kind_seq_braket   TB/numerics_cuda.cuh:10-13
 //   bases_of_uniform_ampl_with_random_phases  TB/numerical.h:120-122 (seeded)
 //   density_of_states_seq              TB/functions.h:15-32
@@ -19,6 +21,7 @@
 #include <map>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <type_traits>
 #include <utility>
 #include <vector>
@@ -176,6 +179,17 @@ class PartialLattice {
   // fills set_scalar_field from a stateful RNG, TB/snippets.h:765-767)
   void set_scalar_disorder(double W, uint64_t seed) { check(tbk_lattice_set_scalar_disorder(h_, W, seed)); }
   void set_scalar_values(const std::vector<double>& V) { check(tbk_lattice_set_scalar_sites(h_, V.data())); }
+  // vacancies, TB/lattice.h:389-418 (remove_atoms_random drawn from `seed`)
+  void remove_atoms(const std::string& atom_name, const std::vector<LatticeVector<Dim>>& i) {
+    std::vector<int32_t> c;
+    c.reserve(i.size() * Dim);
+    for (const auto& v : i)
+      for (int d = 0; d < Dim; ++d) c.push_back(v[d]);
+    check(tbk_lattice_remove_atoms(h_, atom_name.c_str(), c.data(), (int64_t)i.size()));
+  }
+  void remove_atoms_random(const std::string& atom_name, int n, uint64_t seed = 0) {
+    check(tbk_lattice_remove_atoms_random(h_, atom_name.c_str(), n, seed));
+  }
   // A(r) = G r + c (TB/lattice.h:495-505)
   void set_gauge_linear(const std::array<double, 9>& G_rowmajor, const Vector3d& c) {
     check(tbk_lattice_set_gauge_linear(h_, G_rowmajor.data(), c.data()));
@@ -238,8 +252,21 @@ inline std::vector<double> Cheb_first_kind_seq_braket(const SparseMatrix& M, int
 }
 }  // namespace cuda
 
-// GreenFunction<Scalar>(N, HE, E_min, E_max): a = (E_max - E_min)/2,
-// b = (E_max + E_min)/2, scaled_HE = (HE - b I)/a on the device.
+// numerical::linalg::matrix_spectral_range_sparse (TB/numerical.h:24-46):
+// extreme eigenvalues {E_min, E_max} of a Hermitian matrix, here by device
+// Lanczos (no 5,000-row cap; Ritz values lie inside the spectrum)
+inline std::pair<double, double> matrix_spectral_range_sparse(const SparseMatrix& A, int iters = 200,
+                                                              uint64_t seed = 0) {
+  double e0 = 0.0, e1 = 0.0;
+  check(tbk_spectral_range(A.handle(), iters, seed, &e0, &e1, nullptr, nullptr, nullptr));
+  return {e0, e1};
+}
+
+// GreenFunction<Scalar> (TB/lattice.h:553-576): b = (E_max + E_min)/2,
+// scaled_HE = (HE - b I)/a on the device, with
+//   GreenFunction(N, HE, E_min, E_max)          a = (E_max - E_min)/2
+//   GreenFunction(N, HE, ref_HE, epsilon=0.01)  range of ref_HE, a = (E_max - E_min)/(2 - epsilon)
+//   GreenFunction(N, HE)                        = GreenFunction(N, HE, HE)
 struct GreenFunction {
   int N;
   double a, b, E_min, E_max;
@@ -247,6 +274,16 @@ struct GreenFunction {
 
   GreenFunction(int N_, const SparseMatrix& HE, double E_min_, double E_max_)
       : N(N_), a((E_max_ - E_min_) / 2), b((E_max_ + E_min_) / 2), E_min(E_min_), E_max(E_max_) {
+    rescale(HE);
+  }
+  GreenFunction(int N_, const SparseMatrix& HE, const SparseMatrix& ref_HE, double epsilon = 0.01) : N(N_) {
+    std::tie(E_min, E_max) = matrix_spectral_range_sparse(ref_HE);
+    a = (E_max - E_min) / (2 - epsilon);
+    b = (E_max + E_min) / 2;
+    rescale(HE);
+  }
+  GreenFunction(int N_, const SparseMatrix& HE) : GreenFunction(N_, HE, HE) {}
+  void rescale(const SparseMatrix& HE) {
     tbk_sparse h = nullptr;
     check(tbk_sparse_rescale(&h, HE.handle(), a, b, nullptr));
     scaled_HE = SparseMatrix(h);
@@ -283,6 +320,25 @@ struct GreenFunction {
     return f;
   }
 };
+
+// sum_k coef[k] T_k(Ht) kets on the device: the Cheb_first_kind_seq_view walk
+// plus host sum of TB/numerical.h:346-361 / TB/snippets.h:194-217 in one call
+inline MatrixXcd cheb_expand(const SparseMatrix& Ht, const std::vector<Complex>& coef, const MatrixXcd& kets,
+                             int precision = TBK_PREC_FP64) {
+  MatrixXcd out(kets.rows, kets.cols);
+  check(tbk_cheb_expand(Ht.handle(), (int32_t)coef.size(), reinterpret_cast<const double*>(coef.data()), kets.cols,
+                        kets.raw(), out.raw(), precision, nullptr));
+  return out;
+}
+// exp(-i HE t) kets for the Hamiltonian of G (HE = a scaled_HE + b)
+inline MatrixXcd time_evolve(const GreenFunction& G, double t, const MatrixXcd& kets, double tol = 1e-15,
+                             int precision = TBK_PREC_FP64) {
+  int32_t k = 0;
+  check(tbk_cheb_evolution_terms(G.a, t, tol, &k));
+  std::vector<Complex> c((size_t)k);
+  check(tbk_cheb_coef_evolution(G.a, G.b, t, k, reinterpret_cast<double*>(c.data())));
+  return cheb_expand(G.scaled_HE, c, kets, precision);
+}
 
 // TB/functions.h:15-32: periodic bare H, G(N, H, E_min - 1e-8, E_max + 1e-8),
 // R random-phase kets, DoS = -f(e) / (R pi) at every e of E_list (scaled units).

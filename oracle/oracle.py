@@ -191,6 +191,25 @@ def cheb_blocks(n, cp, ri, v, n_mom, x0):
     return out
 
 
+def cheb_expand(n, cp, ri, v, coef, x0):
+    """sum_k coef[k] T_k(H) x0: the Cheb_first_kind_seq_view walk with a host
+    sum (TB/numerical.h:346-361, used as in TB/snippets.h:194-217)."""
+    blocks = cheb_blocks(n, cp, ri, v, len(coef), x0)        # (K, R, n)
+    out = np.tensordot(np.asarray(coef, dtype=np.complex128), blocks, axes=(0, 0))
+    return np.asfortranarray(out.T)
+
+
+def delta_coefficients(e, N):
+    """a_d(k) T_k(e) for k = 0 .. N, the view loop of TB/snippets.h:194-202
+    (Cheb_first_kind_seq_view(e, 1.) yields T_0 .. T_N before i reaches N)."""
+    t0, t1 = 1.0, e
+    c = []
+    for k in range(N + 1):
+        c.append((1.0 if k == 0 else 2.0) * t0)
+        t0, t1 = t1, 2.0 * e * t1 - t0
+    return np.asarray(c, dtype=np.complex128)
+
+
 def kernel_seq(kind, N, p0=0.0, p1=0.0):
     g = np.zeros(N)
     lib().tbo_kernel_seq(kind, N, p0, p1, _p(g))

@@ -11,6 +11,9 @@
 //      kets to 1e-12
 //   5. DosServer: a double-float request equals the FP64 solve to 1e-10, and
 //      the same request twice gives the same bits
+//   6. GreenFunction(N, H): the Lanczos range of a ring is [-2, 2] (1e-8) and
+//      a = 4 / (2 - 0.01)
+//   7. time_evolve on the ring: plane wave k picks up exp(-i 2 cos(k) t) (1e-11)
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -146,6 +149,35 @@ int main() {
     }
     expect(ma.size() == 96 && err <= 1e-10, "server (double-float) equals the FP64 solve", err);
     expect(same == 0.0, "the same request twice gives the same bits", same);
+  }
+  // ---- 6. bound-free GreenFunction: Lanczos spectral range
+  {
+    UnitCell<1> chain({{1, 0, 0}}, {{"A", {0, 0, 0}}});
+    chain.add_hopping("A", 1, Complex(1.0, 0.0));
+    PartialLattice<1> X(chain, {96});
+    SparseMatrix H = X.get_Hamiltonian_periodic_extend_bare_sparse<double>({1});
+    GreenFunction G(64, H);
+    const double err = std::fmax(std::fabs(G.E_min + 2.0), std::fabs(G.E_max - 2.0));
+    expect(err <= 1e-8, "GreenFunction(N, H) range of the ring", err);
+    expect(std::fabs(G.a - 4.0 / 1.99) <= 1e-8, "GreenFunction(N, H) contraction epsilon 0.01", G.a);
+  }
+  // ---- 7. time evolution of a plane wave on the ring
+  {
+    const int L = 96;
+    UnitCell<1> chain({{1, 0, 0}}, {{"A", {0, 0, 0}}});
+    chain.add_hopping("A", 1, Complex(1.0, 0.0));
+    PartialLattice<1> X(chain, {L});
+    SparseMatrix H = X.get_Hamiltonian_periodic_extend_bare_sparse<double>({1});
+    GreenFunction G(16, H, -2.1, 2.1);
+    const int q = 7;
+    const double kq = 2 * pi * q / L, t = 4.5;
+    MatrixXcd psi(L, 1);
+    for (int i = 0; i < L; ++i) psi(i, 0) = std::polar(1.0 / std::sqrt((double)L), kq * i);
+    MatrixXcd out = time_evolve(G, t, psi);
+    const Complex ph = std::polar(1.0, -2.0 * std::cos(kq) * t);
+    double err = 0.0;
+    for (int i = 0; i < L; ++i) err = std::fmax(err, std::abs(out(i, 0) - ph * psi(i, 0)));
+    expect(err <= 1e-11, "time_evolve plane wave phase", err);
   }
   std::printf("%s\n", failures ? "FAILED" : "ALL PASSED");
   return failures ? 1 : 0;

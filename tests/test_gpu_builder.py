@@ -188,3 +188,21 @@ def test_config_sizes_counts(gpu):
     X3.set_scalar_disorder(2.0, 4)
     H3 = X3.get_Hamiltonian_periodic_extend_bare_sparse([1, 1, 1], float)
     assert H3.nnz == counts["fcc_128_pbc_disorder"]["nnz_H"]
+
+
+def test_builder_random_vacancies_device_compaction(gpu):
+    """remove_atoms_random on both sublattices of a 256 x 192 honeycomb: the
+    device prefix-sum compaction gives the oracle's index_c build bit-exact."""
+    tb = gpu
+    cell = tb.Honeycomb().add_hopping("A", 1, -2.7)
+    X = tb.PartialLattice(cell, (256, 192))
+    X.remove_atoms_random("A", 2500, seed=3)
+    X.remove_atoms_random("B", 1800, seed=4)
+    removed = X.removed_sites()
+    assert int(removed.sum()) == 4300
+    H = X.get_Hamiltonian_sparse(float)
+    spec = spec_from(cell, (256, 192), mode=orc.MODE_SPARSE, is_complex=False, removed=removed.astype(np.int32))
+    _assert_same(H, orc.build_csc(spec))
+    n_kept = X.get_kept_number()
+    cp = H.to_csc()[0]
+    assert n_kept == 2 * 256 * 192 - 4300 and cp[n_kept] == cp[-1]

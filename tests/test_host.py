@@ -93,3 +93,54 @@ def test_lattice_index_scheme(tb):
     assert pos.shape == (30, 3)
     assert np.allclose(pos[X.index_bare((1, 2), 1)], np.array([1.5, -np.sqrt(3) / 2, 0]) * 1
                        + np.array([1.5, np.sqrt(3) / 2, 0]) * 2 + np.array([1, 0, 0]))
+
+
+def test_remove_atoms_host_rules(tb):
+    """remove_atoms / remove_atoms_random (TB/lattice.h:389-418) on the host:
+    index_bare placement, seeded distinct draws on one sublattice, the
+    reference's error texts, and index_c (TB/lattice.h:446-457)."""
+    X = tb.PartialLattice(tb.Honeycomb(), (6, 5))
+    X.remove_atoms("B", [(0, 0), (2, 3), (5, 4)])
+    r = X.removed_sites()
+    assert set(np.flatnonzero(r)) == {X.index_bare((0, 0), 1), X.index_bare((2, 3), 1), X.index_bare((5, 4), 1)}
+    assert X.get_kept_number() == 57
+    c = X.index_comp()
+    assert c[X.index_bare((0, 0), 1)] == -1 and c[0] == 0 and c[2] == 1 and c.max() == 56
+    Y = tb.PartialLattice(tb.Honeycomb(), (64, 48))
+    Y.remove_atoms_random("A", 700, seed=5)
+    m = Y.removed_sites()
+    idx = np.flatnonzero(m)
+    assert len(idx) == 700 and np.all(idx % 2 == 0)
+    Z = tb.PartialLattice(tb.Honeycomb(), (64, 48))
+    Z.remove_atoms_random("A", 700, seed=5)
+    assert np.array_equal(Z.removed_sites(), m)
+    Z.remove_sites(np.zeros(Z.get_total_number(), np.uint8))
+    Z.remove_atoms_random("A", 700, seed=6)
+    assert not np.array_equal(Z.removed_sites(), m)
+    # all cells: every A removed
+    W = tb.PartialLattice(tb.Honeycomb(), (4, 4))
+    W.remove_atoms_random("B", 16, seed=1)
+    assert np.array_equal(np.flatnonzero(W.removed_sites()), np.arange(1, 32, 2))
+    with pytest.raises(tb.TbkError, match="does not exist in the unit cell"):
+        X.remove_atoms("Q", [(0, 0)])
+    with pytest.raises(tb.TbkError, match="larger than the total number"):
+        W.remove_atoms_random("A", 17)
+    with pytest.raises(tb.TbkError, match="outside the lattice"):
+        X.remove_atoms("A", [(6, 0)])
+
+
+def test_expansion_coefficients_host(tb):
+    """Host coefficient helpers of the vector expansions: the sawtooth delta
+    projection (TB/snippets.h:194-202) against the oracle's loop, and
+    exp(-i H t) against scipy's Bessel J."""
+    import oracle as orc
+    special = pytest.importorskip("scipy.special")
+    for e, N in ((0.3, 10), (-0.97, 200), (0.0, 1)):
+        assert np.allclose(tb.delta_coefficients(e, N), orc.delta_coefficients(e, N), rtol=1e-13, atol=1e-13)
+    for a, b, t in ((2.0, 0.3, 5.0), (4.6, -0.1, 0.0), (8.6, 0.0, -3.0)):
+        c = tb.evolution_coefficients(a, b, t)
+        k = np.arange(len(c))
+        ref = np.exp(-1j * b * t) * (2.0 - (k == 0)) * (-1j) ** k * special.jv(k, a * t)
+        assert np.max(np.abs(c - ref)) <= 1e-14
+        assert abs(special.jv(len(c), a * t)) < 1e-15
+    assert tb.evolution_terms(1.0, 100.0) > 100

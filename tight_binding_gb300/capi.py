@@ -50,6 +50,18 @@ class ServerConfig(C.Structure):
                 ("max_resident", C.c_int32), ("result_arena_mb", C.c_int32), ("step_gb", C.c_double)]
 
 
+class MomentsHeader(C.Structure):
+    """tbk_moments_header (256 bytes)"""
+    _fields_ = [("magic", C.c_char * 8), ("version", C.c_int32), ("kind", C.c_int32), ("rows", C.c_int32),
+                ("cols", C.c_int32), ("is_complex", C.c_int32), ("R", C.c_int32), ("precision", C.c_int32),
+                ("kernel", C.c_int32), ("seed", C.c_uint64), ("e_min", C.c_double), ("e_max", C.c_double),
+                ("kernel_p0", C.c_double), ("kernel_p1", C.c_double), ("n_sites", C.c_int64),
+                ("checksum", C.c_uint64), ("label", C.c_char * 160)]
+
+
+MOMENTS_DOS, MOMENTS_MU_NM, MOMENTS_V_NM = 1, 2, 3
+
+
 class Request(C.Structure):
     """tbk_request"""
     _fields_ = [("lattice", C.c_void_p), ("build_mode", C.c_int32), ("extend", C.c_int32 * 3),
@@ -83,6 +95,9 @@ SIGNATURES = {
     "tbk_lattice_set_scalar_sites": (C.c_int, [_vp, _pd]),
     "tbk_lattice_set_scalar_disorder": (C.c_int, [_vp, _d, _u64]),
     "tbk_lattice_set_removed": (C.c_int, [_vp, _pu8]),
+    "tbk_lattice_remove_atoms": (C.c_int, [_vp, C.c_char_p, _pi32, _i64]),
+    "tbk_lattice_remove_atoms_random": (C.c_int, [_vp, C.c_char_p, _i64, _u64]),
+    "tbk_lattice_get_removed": (C.c_int, [_vp, _pu8]),
     "tbk_lattice_kept_number": (C.c_int, [_vp, _pi64]),
     "tbk_build_hamiltonian": (C.c_int, [C.POINTER(_vp), _vp, _i32, _pi32, _i32, _vp]),
     "tbk_build_position": (C.c_int, [C.POINTER(_vp), _vp, _i32, _vp]),
@@ -92,6 +107,14 @@ SIGNATURES = {
     "tbk_sparse_destroy": (None, [_vp]),
     "tbk_sparse_rescale": (C.c_int, [C.POINTER(_vp), _vp, _d, _d, _vp]),
     "tbk_sparse_commutator": (C.c_int, [C.POINTER(_vp), _vp, _vp, _vp]),
+    "tbk_spectral_range": (C.c_int, [_vp, _i32, _u64, _pd, _pd, _pd, _pd, _vp]),
+    "tbk_cheb_expand": (C.c_int, [_vp, _i32, _vp, _i32, _vp, _vp, _i32, _vp]),
+    "tbk_moments_save": (C.c_int, [_cp, _vp, _vp]),
+    "tbk_moments_load_header": (C.c_int, [_cp, _vp]),
+    "tbk_moments_load": (C.c_int, [_cp, _vp, _vp, _i64]),
+    "tbk_cheb_coef_delta": (C.c_int, [C.c_double, _i32, _vp]),
+    "tbk_cheb_coef_evolution": (C.c_int, [C.c_double, C.c_double, C.c_double, _i32, _vp]),
+    "tbk_cheb_evolution_terms": (C.c_int, [C.c_double, C.c_double, C.c_double, _pi32]),
     "tbk_cheb_braket_real": (C.c_int, [_i32, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _i32, _i32, _vp]),
     "tbk_cheb_braket_complex": (C.c_int, [_i32, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _i32, _i32, _vp]),
     "tbk_kpm_create": (C.c_int, [C.POINTER(_vp), _vp, _i32, _i32]),

@@ -115,6 +115,43 @@ int sm_count() {
   return sms;
 }
 
+// ------------------------------------------------------------------ vacancies
+__global__ void keep_flags_kernel(int64_t n, const uint8_t* __restrict__ removed, int32_t* __restrict__ keep) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    keep[i] = removed[i] ? 0 : 1;
+}
+__global__ void scatter_comp_kernel(int64_t n, const uint8_t* __restrict__ removed, const int32_t* __restrict__ pos,
+                                    int32_t* __restrict__ comp, int32_t* __restrict__ inv) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (removed[i]) {
+      comp[i] = -1;
+    } else {
+      comp[i] = pos[i];
+      inv[pos[i]] = (int32_t)i;
+    }
+  }
+}
+
+// bare -> compressed site map (comp, -1 where removed) and compressed -> bare
+// (inv) from the removal mask: keep flags, exclusive scan, scatter
+int compact_sites(const uint8_t* removed_host, int64_t n, DevBuf* comp, DevBuf* inv, int32_t* kept, cudaStream_t st) {
+  DevBuf mask, keep, pos;
+  TBK_TRY(mask.alloc(n));
+  TBK_TRY(keep.alloc(sizeof(int32_t) * n));
+  TBK_TRY(pos.alloc(sizeof(int32_t) * n));
+  TBK_TRY(comp->alloc(sizeof(int32_t) * n));
+  TBK_TRY(inv->alloc(sizeof(int32_t) * (n + 1)));
+  TBK_CUDA(cudaMemcpyAsync(mask.p, removed_host, n, cudaMemcpyHostToDevice, st));
+  const int g = std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * sm_count()));
+  keep_flags_kernel<<<g, 256, 0, st>>>(n, mask.as<uint8_t>(), keep.as<int32_t>());
+  TBK_CHECK_LAUNCH();
+  TBK_TRY(exclusive_scan_i32(keep.as<int32_t>(), pos.as<int32_t>(), n, st, kept));
+  scatter_comp_kernel<<<g, 256, 0, st>>>(n, mask.as<uint8_t>(), pos.as<int32_t>(), comp->as<int32_t>(),
+                                         inv->as<int32_t>());
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
+}
+
 // ------------------------------------------------------------------ builder
 constexpr int kMaxCand = 64;   // triplets landing in one CSC column
 
@@ -685,20 +722,13 @@ int tbk_build_hamiltonian(tbk_sparse* out, tbk_lattice L, int32_t mode, const in
     P.scalar_sites = dscalar.as<double>();
   }
   P.n_kept = P.n_cols;
-  std::vector<int32_t> comp, inv;
   if (mode == TBK_BUILD_SPARSE && !L->removed.empty()) {
-    // index_comp_construct, TB/lattice.h:447-457
-    comp.resize(L->total);
-    int32_t c = 0;
-    for (int64_t i = 0; i < L->total; ++i) {
-      if (L->removed[i]) comp[i] = -1;
-      else { comp[i] = c++; inv.push_back((int32_t)i); }
-    }
-    P.n_kept = c;
-    TBK_TRY(dcomp.alloc(sizeof(int32_t) * comp.size()));
-    TBK_TRY(dinv.alloc(sizeof(int32_t) * (inv.size() + 1)));
-    TBK_CUDA(cudaMemcpyAsync(dcomp.p, comp.data(), dcomp.bytes, cudaMemcpyHostToDevice, st));
-    if (!inv.empty()) TBK_CUDA(cudaMemcpyAsync(dinv.p, inv.data(), sizeof(int32_t) * inv.size(), cudaMemcpyHostToDevice, st));
+    // index_comp_construct (TB/lattice.h:447-457) as a device compaction: the
+    // site mask goes up once, kept flags are prefix-summed, and the bare ->
+    // compressed map (-1 = removed) and its inverse are scattered from the scan
+    int32_t kept = 0;
+    TBK_TRY(compact_sites(L->removed.data(), L->total, &dcomp, &dinv, &kept, st));
+    P.n_kept = kept;
     P.comp = dcomp.as<int32_t>();
     P.inv = dinv.as<int32_t>();
   }

@@ -327,6 +327,61 @@ int tbk_lattice_set_removed(tbk_lattice L, const uint8_t* removed) {
   return TBK_OK;
 }
 
+static int lattice_atom(tbk_lattice L, const char* atom, const char* fn, int* a) {
+  if (!L || !atom) return fail(TBK_ERR_INVALID, "%s: null argument", fn);
+  for (size_t i = 0; i < L->cell.names.size(); ++i)
+    if (L->cell.names[i] == atom) { *a = (int)i; return TBK_OK; }
+  return fail(TBK_ERR_INVALID, "Atom %s does not exist in the unit cell.", atom);
+}
+
+int tbk_lattice_remove_atoms(tbk_lattice L, const char* atom, const int32_t* cells, int64_t n) {
+  int a = 0;
+  TBK_TRY(lattice_atom(L, atom, "tbk_lattice_remove_atoms", &a));
+  if (n < 0 || (n > 0 && !cells)) return fail(TBK_ERR_INVALID, "tbk_lattice_remove_atoms: bad cell list");
+  const int dim = L->cell.dim, na = L->cell.n_atoms;
+  std::vector<int64_t> idx((size_t)n);
+  for (int64_t k = 0; k < n; ++k) {
+    // index_bare(i_v, a) = i_v . span_s + a (row-major cells, atom fastest)
+    int64_t c = 0;
+    for (int i = 0; i < dim; ++i) {
+      const int32_t v = cells[k * dim + i];
+      if (v < 0 || v >= L->span[i])
+        return fail(TBK_ERR_INVALID, "tbk_lattice_remove_atoms: cell %lld outside the lattice", (long long)k);
+      c = c * L->span[i] + v;
+    }
+    idx[(size_t)k] = c * na + a;
+  }
+  if (L->removed.empty()) L->removed.assign((size_t)L->total, 0);
+  for (int64_t b : idx) L->removed[(size_t)b] = 1;
+  return TBK_OK;
+}
+
+int tbk_lattice_remove_atoms_random(tbk_lattice L, const char* atom, int64_t n, uint64_t seed) {
+  int a = 0;
+  TBK_TRY(lattice_atom(L, atom, "tbk_lattice_remove_atoms_random", &a));
+  const int64_t cells = L->total / L->cell.n_atoms;
+  if (n < 0 || n > cells) return fail(TBK_ERR_INVALID, "The random selection is larger than the total number.");
+  // n distinct cells out of `cells`, seeded: Floyd's sampling (Bentley & Floyd,
+  // CACM 30(9), 1987) -- for j = cells-n .. cells-1 draw t in [0, j]; take t,
+  // or j when t is already taken.  The draws are the counter-based u01 stream.
+  std::set<int64_t> pick;
+  for (int64_t j = cells - n; j < cells; ++j) {
+    int64_t t = (int64_t)(tbk::u01(seed, tbk::kRemoveStream, (uint64_t)j) * (double)(j + 1));
+    if (t > j) t = j;
+    if (!pick.insert(t).second) pick.insert(j);
+  }
+  if (L->removed.empty()) L->removed.assign((size_t)L->total, 0);
+  for (int64_t c : pick) L->removed[(size_t)(c * L->cell.n_atoms + a)] = 1;
+  return TBK_OK;
+}
+
+int tbk_lattice_get_removed(tbk_lattice L, uint8_t* out) {
+  if (!L || !out) return fail(TBK_ERR_INVALID, "tbk_lattice_get_removed: null argument");
+  if (L->removed.empty()) std::memset(out, 0, (size_t)L->total);
+  else std::memcpy(out, L->removed.data(), (size_t)L->total);
+  return TBK_OK;
+}
+
 int tbk_lattice_kept_number(tbk_lattice L, int64_t* n) {
   if (!L || !n) return fail(TBK_ERR_INVALID, "tbk_lattice_kept_number: null argument");
   int64_t k = L->total;

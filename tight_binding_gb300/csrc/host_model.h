@@ -31,6 +31,7 @@ TBK_HD double u01(uint64_t seed, uint64_t stream, uint64_t idx) {
   return (double)(h >> 11) * 0x1.0p-53;
 }
 constexpr uint64_t kDisorderStream = 0xD150D3Dull;
+constexpr uint64_t kRemoveStream = 0x5ACA7C1Eull;   // remove_atoms_random draws
 
 struct Hop {
   int32_t from, to;

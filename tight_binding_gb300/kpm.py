@@ -4,6 +4,8 @@
     bases_of_uniform_ampl_with_random_phases   TB/numerical.h:120-122 (seeded)
     kernel_seq / kernels            TB/numerical.h:393-447
     GreenFunction, GreenFunctionImag   TB/lattice.h:532-652
+    spectral_range                  TB/numerical.h:24-46 (device Lanczos, no size cap)
+    cheb_expand, time_evolve        Cheb_first_kind_seq_view sums, TB/numerical.h:346-361
     density_of_states_seq / _function  TB/functions.h:5-32
     KpmSolver                       resident plan (H~ and recursion state on the GPU)
 """
@@ -197,14 +199,44 @@ class GreenFunctionImag:
         return int(round(math.acos(e_max) / math.pi * N)), int(round(math.acos(e_min) / math.pi * N))
 
 
-class GreenFunction:
-    """GreenFunction<Scalar>(N, HE, E_min, E_max), TB/lattice.h:553-559: a, b and
-    scaled_HE = (HE - b I)/a computed in FP64 on the device."""
+def spectral_range(A: SparseMatrix, iters: int = 200, seed: int = 0) -> tuple[float, float, float, float]:
+    """(E_min, E_max, res_min, res_max) of a Hermitian matrix by `iters` device
+    Lanczos steps: the extreme Ritz values and their residual norms (an
+    eigenvalue lies within res of each).  Replaces the reference's CPU Spectra
+    solve matrix_spectral_range_sparse (TB/numerical.h:24-46), which refuses
+    matrices above 5,000 rows; Ritz values lie inside the spectrum, so callers
+    keep a margin (GreenFunction's epsilon)."""
+    e0, e1, r0, r1 = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+    check(lib().tbk_spectral_range(A.handle, int(iters), int(seed), C.byref(e0), C.byref(e1), C.byref(r0),
+                                   C.byref(r1), None))
+    return e0.value, e1.value, r0.value, r1.value
 
-    def __init__(self, N: int, HE: SparseMatrix, E_min: float, E_max: float):
+
+class GreenFunction:
+    """GreenFunction<Scalar>, TB/lattice.h:553-576: a, b and scaled_HE = (HE - b I)/a
+    computed in FP64 on the device.  The three constructors:
+
+        GreenFunction(N, HE, E_min, E_max)         a = (E_max - E_min)/2
+        GreenFunction(N, HE, ref_HE, epsilon=0.01) range of ref_HE by Lanczos,
+                                                   a = (E_max - E_min)/(2 - epsilon)
+        GreenFunction(N, HE)                       = GreenFunction(N, HE, HE)
+
+    (the third also tabulates dense T_n(H~) below 5,000 rows in the reference,
+    TB/lattice.h:571-576; that dense table is not built here)."""
+
+    def __init__(self, N: int, HE: SparseMatrix, E_min=None, E_max=None, epsilon: float | None = None,
+                 lanczos_iters: int = 200):
         self.N = N
+        if E_min is None or isinstance(E_min, SparseMatrix):
+            ref = HE if E_min is None else E_min
+            eps = 0.01 if epsilon is None else float(epsilon)
+            if E_max is not None:          # GreenFunction(N, HE, ref_HE, epsilon) positionally
+                eps = float(E_max)
+            E_min, E_max, _, _ = spectral_range(ref, lanczos_iters)
+            self.a = (E_max - E_min) / (2 - eps)
+        else:
+            self.a = (E_max - E_min) / 2
         self.E_min, self.E_max = E_min, E_max
-        self.a = (E_max - E_min) / 2
         self.b = (E_max + E_min) / 2
         h = C.c_void_p()
         check(lib().tbk_sparse_rescale(C.byref(h), HE.handle, self.a, self.b, None))
@@ -218,6 +250,53 @@ class GreenFunction:
 
     def imag(self, bras, kets, precision="fp64", kernel: Kernel | None = None) -> GreenFunctionImag:
         return GreenFunctionImag(self, bras, kets, precision=precision, kernel=kernel)
+
+
+# ------------------------------------------------------ expansions applied to vectors
+def cheb_expand(Ht: SparseMatrix, coef, kets, precision="fp64") -> np.ndarray:
+    """sum_k coef[k] T_k(Ht) kets on the device (kets: n or n x R complex;
+    returns the same shape).  The walk the reference writes with
+    Cheb_first_kind_seq_view (TB/numerical.h:346-361) plus a host sum."""
+    kets = np.asarray(kets)
+    n = Ht.shape[0]
+    K = _block(kets, n)
+    c = np.ascontiguousarray(coef, dtype=np.complex128)
+    out = np.zeros(K.shape, dtype=np.complex128, order="F")
+    check(lib().tbk_cheb_expand(Ht.handle, len(c), capi.ptr(c), K.shape[1], capi.ptr(K), capi.ptr(out),
+                                _prec(precision), None))
+    return out.reshape(kets.shape) if kets.ndim == 1 else out
+
+
+def sparse_apply(A: SparseMatrix, kets, precision="fp64") -> np.ndarray:
+    """A @ kets on the device (T_1(A) kets)."""
+    return cheb_expand(A, [0.0, 1.0], kets, precision)
+
+
+def delta_coefficients(e: float, N: int) -> np.ndarray:
+    """a_d(k) T_k(e), k = 0 .. N: the single-energy projection of
+    conductivity_test_sawtooth (TB/snippets.h:175, 194-202)."""
+    c = np.zeros(N + 1, dtype=np.complex128)
+    check(lib().tbk_cheb_coef_delta(float(e), int(N), capi.ptr(c)))
+    return c
+
+
+def evolution_terms(a: float, t: float, tol: float = 1e-15) -> int:
+    k = C.c_int32()
+    check(lib().tbk_cheb_evolution_terms(float(a), float(t), float(tol), C.byref(k)))
+    return k.value
+
+
+def evolution_coefficients(a: float, b: float, t: float, n_terms: int | None = None, tol: float = 1e-15) -> np.ndarray:
+    """exp(-i H t), H = a Ht + b: exp(-i b t) (2 - delta_k0) (-i)^k J_k(a t)."""
+    n_terms = evolution_terms(a, t, tol) if n_terms is None else int(n_terms)
+    c = np.zeros(n_terms, dtype=np.complex128)
+    check(lib().tbk_cheb_coef_evolution(float(a), float(b), float(t), n_terms, capi.ptr(c)))
+    return c
+
+
+def time_evolve(G: "GreenFunction", t: float, kets, precision="fp64", tol: float = 1e-15) -> np.ndarray:
+    """exp(-i HE t) kets for the Hamiltonian of G (HE = a scaled_HE + b)."""
+    return cheb_expand(G.scaled_HE, evolution_coefficients(G.a, G.b, t, tol=tol), kets, precision)
 
 
 # ------------------------------------------------------------------ DoS entry points

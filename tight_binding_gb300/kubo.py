@@ -4,6 +4,7 @@
     conductivity_Kubo_Bastin      sigma_xy, TB/snippets.h:306-456
     conductivity_spectrum         Kubo-Greenwood sigma_xx(E), TB/snippets.h:225-304
     generate_V_moments            explicit velocity moments, TB/snippets.h:491-518
+    conductivity_test_sawtooth    single-energy delta projection, TB/snippets.h:173-223
 """
 from __future__ import annotations
 
@@ -127,6 +128,27 @@ def conductivity_spectrum(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMa
                  recursion=recursion)
     eps = chebyshev_nodes(N)
     return eps, greenwood_sigma(mu, eps, R), mu
+
+
+def conductivity_test_sawtooth(X: PartialLattice, N: int, E: float, R: int = 4, seed: int = 0,
+                               precision="fp64") -> float:
+    """TB/snippets.h:173-223: single-energy Kubo-Greenwood value of a sawtooth
+    chain.  Real open-BC H, G(N, H, 4t - 2 - 1e-6, 4t + 1e-6) with t = -E/2,
+    e = G.scale(E); v_x = X H~ - H~ X; D = sum_{k=0..N} a_d(k) T_k(e) T_k(H~)
+    (the view loop runs N + 1 terms); returns Re tr(<v_x D v_x r | D r>) / R.
+    Kets: R seeded random-phase vectors (the reference draws unseeded ones)."""
+    from .kpm import bases_of_uniform_ampl_with_random_phases, cheb_expand, delta_coefficients, sparse_apply
+    H_og = X.get_Hamiltonian_sparse(float)
+    t = -E / 2.0
+    G = GreenFunction(N, H_og, 4 * t - 2.0 - 1e-6, 4 * t + 1e-6)
+    e = G.scale(E, 1.0)
+    H = G.scaled_HE
+    v_x = commutator(H, X.op_position(0))
+    kets = bases_of_uniform_ampl_with_random_phases(X.get_total_number(), R, seed)
+    coef = delta_coefficients(e, N)
+    kets_R = cheb_expand(H, coef, kets, precision)
+    kets_L = sparse_apply(v_x, cheb_expand(H, coef, sparse_apply(v_x, kets), precision))
+    return float(np.sum(kets_L.real * kets_R.real + kets_L.imag * kets_R.imag)) / R
 
 
 def generate_V_moments(X: PartialLattice, N: int, R: int = 100, seed: int = 0, tensor: bool = False) -> np.ndarray:

@@ -241,9 +241,38 @@ class PartialLattice:
         """Anderson disorder V = W (u - 1/2), generated on the device."""
         check(lib().tbk_lattice_set_scalar_disorder(self._h, float(W), int(seed)))
 
+    # -- vacancies (TB/lattice.h:389-464)
     def remove_sites(self, removed) -> None:
+        """Replace the removal flags with `removed` (N bare sites, nonzero = removed)."""
         r = np.ascontiguousarray(removed, dtype=np.uint8)
         check(lib().tbk_lattice_set_removed(self._h, r.ctypes.data_as(C.POINTER(C.c_uint8))))
+
+    def remove_atoms(self, atom_name: str, cells) -> None:
+        """remove_atoms(atom_name, i), TB/lattice.h:389-402: the atom of every listed cell."""
+        c = np.ascontiguousarray(np.asarray(cells, dtype=np.int32).reshape(-1, self.dim))
+        check(lib().tbk_lattice_remove_atoms(self._h, atom_name.encode(), capi.as_i32p(c), c.shape[0]))
+
+    def remove_atoms_random(self, atom_name: str, n: int, seed: int = 0) -> None:
+        """remove_atoms_random(atom_name, n), TB/lattice.h:404-418, from a seeded
+        stream (the reference draws from std::random_device)."""
+        check(lib().tbk_lattice_remove_atoms_random(self._h, atom_name.encode(), int(n), int(seed)))
+
+    def removed_sites(self) -> np.ndarray:
+        r = np.zeros(self.get_total_number(), dtype=np.uint8)
+        check(lib().tbk_lattice_get_removed(self._h, r.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return r
+
+    def index_comp(self) -> np.ndarray:
+        """index_c, TB/lattice.h:446-457: bare -> compressed index, -1 where removed."""
+        keep = self.removed_sites() == 0
+        c = np.full(keep.shape, -1, dtype=np.int32)
+        c[keep] = np.arange(int(keep.sum()), dtype=np.int32)
+        return c
+
+    def get_kept_number(self) -> int:
+        n = C.c_int64()
+        check(lib().tbk_lattice_kept_number(self._h, C.byref(n)))
+        return n.value
 
     # -- builders (TB/lattice.h:216-377)
     def _build(self, mode: int, extend, scalar) -> SparseMatrix:
