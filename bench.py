@@ -586,6 +586,38 @@ def run_gemm(args):
     return 0
 
 
+def run_expand(args):
+    """exp(-i H t) applied to R = 8 random-phase vectors on the benchmark
+    honeycomb (--cells^2 cells, disorder seed 1) through tbk_cheb_expand, in
+    --precision, host vectors in and out (end to end, wall clock).  Algorithmic
+    bytes per term: H~ once (ELL off-diagonal index + value, diagonal value),
+    the recursion's three vector streams and the complex128 accumulator
+    (read + write) plus the re-read of the new term."""
+    import tight_binding_gb300 as tb
+
+    X = tb.PartialLattice(tb.Honeycomb().add_hopping("A", 1, T_HOP), (args.cells, args.cells))
+    X.set_scalar_disorder(W_DIS, 1)
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], float)
+    G = tb.GreenFunction(16, H, -BOUND, BOUND)
+    n = H.shape[0]
+    R = 8
+    kets = tb.bases_of_uniform_ampl_with_random_phases(n, R, 0)
+    coef = tb.evolution_coefficients(G.a, G.b, args.expand)
+    tb.cheb_expand(G.scaled_HE, coef[:4], kets, args.precision)          # warm-up (ELL, modules)
+    t0 = time.perf_counter()
+    out = tb.cheb_expand(G.scaled_HE, coef, kets, args.precision)
+    dt = time.perf_counter() - t0
+    csz = {"mixed": 8, "fp64": 16, "dd": 32}[args.precision]
+    vsz = {"mixed": 4, "fp64": 8, "dd": 16}[args.precision]
+    nnz_off = 3 * n
+    per_term = nnz_off * (4 + vsz) + n * vsz + n * R * (3 * csz + csz + 32)
+    print(json.dumps({"expand": "exp(-iHt)", "t": args.expand, "terms": len(coef), "sites": n, "R": R,
+                      "precision": args.precision, "s_e2e": dt,
+                      "updates_per_s": n * R * len(coef) / dt, "GBps_e2e": per_term * len(coef) / dt / 1e9,
+                      "norm_err": float(np.max(np.abs(np.linalg.norm(out, axis=0) - 1.0)))}), flush=True)
+    return 0
+
+
 def run_kernel_only(args):
     """Small case of the same kernel for ncu captures: one mixed-precision DoS
     solve (doubling) on a honeycomb of --cells^2 cells, R = 32."""
@@ -642,7 +674,11 @@ def main():
                     help="one honeycomb --cells^2 request through the server (profiling case)")
     ap.add_argument("--gemm", type=int, nargs=2, metavar=("M", "K"),
                     help="mu_nm GEMM alone on random M x K complex blocks (profiling case)")
+    ap.add_argument("--expand", type=float, default=None, metavar="T",
+                    help="time evolution exp(-iHt) of 8 vectors to time T (vector-expansion leg)")
     args = ap.parse_args()
+    if args.expand is not None:
+        return run_expand(args)
     if args.gemm:
         return run_gemm(args)
     if args.serve_single:
