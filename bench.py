@@ -61,6 +61,25 @@ def dist_info():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, ws: int, device=None) -> float:
+    """The job's time: the maximum of every rank's value (all-reduce MAX over
+    the default process group; the value itself at world size 1)."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, ws: int, steps: int, total_ms: float) -> float:
+    """Whole-job throughput of weakly scaled replicas: every rank processes
+    units_per_rank per step; the job takes the slowest rank's time."""
+    return ws * units_per_rank * steps / (total_ms / 1e3)
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -248,12 +267,9 @@ def run_gpu(args):
     clocks = sampler.stop()
     per_step = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     total_ms = ev[0].elapsed_time(ev[-1])
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, ws, dev)
     updates = float(N) * M_MOM * R_VEC
-    value = ws * updates * args.steps / (total_ms / 1e3)
+    value = job_rate(updates, ws, args.steps, total_ms)
 
     if rank != 0:
         if ws > 1:
