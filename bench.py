@@ -357,9 +357,13 @@ def run_gpu(args):
     # ---- CPU baseline: oracle on a bounded sample (all host cores)
     threads = os.cpu_count() or 1
     cpu_val, cpu_dt = cpu_sample(cp, ri, v, N, args.cpu_steps, threads)
+    one_steps = max(2, args.cpu_steps // 16)
+    one_val, one_dt = cpu_sample(cp, ri, v, N, one_steps, 1)
     cpu = {"value": cpu_val, "unit": UNIT, "cores": threads, "kind": "port",
            "sample": f"{args.cpu_steps} recursion steps x 32 vectors of the same H~ ({cpu_dt:.1f} s), "
-                     f"C restatement of TB/numerical.h:363-381, OpenMP over vectors"}
+                     f"C restatement of TB/numerical.h:363-381, OpenMP over vectors",
+           "single_thread": {"value": one_val, "cores": 1, "sample": f"{one_steps} steps x 32 vectors ({one_dt:.1f} s), "
+                             "the serial product the reference's Eigen path runs"}}
 
     launches_per_step = 1 + rec_launch + 2 + 2     # load kets, recursion, reduce+assemble, kernel+rho
     line = {
