@@ -51,7 +51,9 @@ def test_cheb_expand_edge_term_counts(gpu):
     Ht = G.scaled_HE
     n = Ht.shape[0]
     kets = tb.bases_of_uniform_ampl_with_random_phases(n, 2, 1)
-    assert np.array_equal(tb.cheb_expand(Ht, [1.0], kets), kets)          # T_0 only
+    assert np.array_equal(tb.cheb_expand(Ht, [1.0], kets, "fp64"), kets)  # T_0 only
+    # double-float vectors carry 48 significant bits
+    assert np.max(np.abs(tb.cheb_expand(Ht, [1.0], kets) - kets)) <= 1e-15
     Hs = _scipy(Ht)
     assert np.allclose(tb.sparse_apply(Ht, kets), Hs @ kets, rtol=0, atol=1e-14)
     assert np.allclose(tb.cheb_expand(Ht, [0.0, 0.0, 1.0], kets), 2 * (Hs @ (Hs @ kets)) - kets, rtol=0, atol=1e-13)

@@ -43,7 +43,10 @@ constexpr int kStepWarps = kStepThreads / 32;
 //                            FIRST: part[1] += <x|H x> (= <v_0|v_1>)
 //   braket:                  part[0] += <b|v_{s+1}>;  FIRST also part[1] += <b|x>
 //   gather == 0: no product at all (the last doubling step only needs the dots).
-template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET>
+//   KST: also write the output into a complex64 K-tiled store (Kubo blocks); a
+//   template flag because even an untaken runtime branch there costs the
+//   moments recursion ~8% of its bandwidth.
+template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET, bool KST = false>
 __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     int32_t n, int32_t n_tiles, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
     const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
@@ -137,7 +140,7 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
       }
     }
     if (store) st_v<F, VPL>(y + me * VPL, out);
-    if (kstore) {
+    if constexpr (KST) {
       // block km of a complex64 K-tiled store (element k of block m at
       // ((k/16)*kM + m)*16 + k%16, k = row * R + vector): one rounding per value
 #pragma unroll
@@ -286,12 +289,15 @@ static int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
   auto b = static_cast<const CT*>(a.bras);
   auto ev = static_cast<const F*>(a.eval);
   auto dg = static_cast<const F*>(a.diag);
-#define TBK_STEP(FI, BR)                                                                   \
-  kpm_step_kernel<F, R, CPLX_H, FI, BR><<<grid, kStepThreads, 0, st>>>(                    \
+#define TBK_STEP(FI, BR, KS)                                                               \
+  kpm_step_kernel<F, R, CPLX_H, FI, BR, KS><<<grid, kStepThreads, 0, st>>>(                \
       a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.kstore, \
       a.kM, a.km)
-  if (first) { if (braket) TBK_STEP(true, true); else TBK_STEP(true, false); }
-  else { if (braket) TBK_STEP(false, true); else TBK_STEP(false, false); }
+  if (a.kstore) {
+    if (braket) return fail(TBK_ERR_UNSUPPORTED, "K-tiled store with a braket step");
+    if (first) TBK_STEP(true, false, true); else TBK_STEP(false, false, true);
+  } else if (first) { if (braket) TBK_STEP(true, true, false); else TBK_STEP(true, false, false); }
+  else { if (braket) TBK_STEP(false, true, false); else TBK_STEP(false, false, false); }
 #undef TBK_STEP
   TBK_CHECK_LAUNCH();
   return TBK_OK;

@@ -253,10 +253,12 @@ class GreenFunction:
 
 
 # ------------------------------------------------------ expansions applied to vectors
-def cheb_expand(Ht: SparseMatrix, coef, kets, precision="fp64") -> np.ndarray:
+def cheb_expand(Ht: SparseMatrix, coef, kets, precision="dd") -> np.ndarray:
     """sum_k coef[k] T_k(Ht) kets on the device (kets: n or n x R complex;
     returns the same shape).  The walk the reference writes with
-    Cheb_first_kind_seq_view (TB/numerical.h:346-361) plus a host sum."""
+    Cheb_first_kind_seq_view (TB/numerical.h:346-361) plus a host sum.
+    precision "dd" (default: double-float recursion, FP64-class accuracy on
+    the FP32 pipe, faster than "fp64" on this GPU), "fp64" or "mixed"."""
     kets = np.asarray(kets)
     n = Ht.shape[0]
     K = _block(kets, n)
@@ -267,7 +269,7 @@ def cheb_expand(Ht: SparseMatrix, coef, kets, precision="fp64") -> np.ndarray:
     return out.reshape(kets.shape) if kets.ndim == 1 else out
 
 
-def sparse_apply(A: SparseMatrix, kets, precision="fp64") -> np.ndarray:
+def sparse_apply(A: SparseMatrix, kets, precision="dd") -> np.ndarray:
     """A @ kets on the device (T_1(A) kets)."""
     return cheb_expand(A, [0.0, 1.0], kets, precision)
 
@@ -294,7 +296,7 @@ def evolution_coefficients(a: float, b: float, t: float, n_terms: int | None = N
     return c
 
 
-def time_evolve(G: "GreenFunction", t: float, kets, precision="fp64", tol: float = 1e-15) -> np.ndarray:
+def time_evolve(G: "GreenFunction", t: float, kets, precision="dd", tol: float = 1e-15) -> np.ndarray:
     """exp(-i HE t) kets for the Hamiltonian of G (HE = a scaled_HE + b)."""
     return cheb_expand(G.scaled_HE, evolution_coefficients(G.a, G.b, t, tol=tol), kets, precision)
 

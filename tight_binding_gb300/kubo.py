@@ -131,7 +131,7 @@ def conductivity_spectrum(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMa
 
 
 def conductivity_test_sawtooth(X: PartialLattice, N: int, E: float, R: int = 4, seed: int = 0,
-                               precision="fp64") -> float:
+                               precision="dd") -> float:
     """TB/snippets.h:173-223: single-energy Kubo-Greenwood value of a sawtooth
     chain.  Real open-BC H, G(N, H, 4t - 2 - 1e-6, 4t + 1e-6) with t = -E/2,
     e = G.scale(E); v_x = X H~ - H~ X; D = sum_{k=0..N} a_d(k) T_k(e) T_k(H~)
@@ -147,7 +147,7 @@ def conductivity_test_sawtooth(X: PartialLattice, N: int, E: float, R: int = 4, 
     kets = bases_of_uniform_ampl_with_random_phases(X.get_total_number(), R, seed)
     coef = delta_coefficients(e, N)
     kets_R = cheb_expand(H, coef, kets, precision)
-    kets_L = sparse_apply(v_x, cheb_expand(H, coef, sparse_apply(v_x, kets), precision))
+    kets_L = sparse_apply(v_x, cheb_expand(H, coef, sparse_apply(v_x, kets, precision), precision), precision)
     return float(np.sum(kets_L.real * kets_R.real + kets_L.imag * kets_R.imag)) / R
 
 
