@@ -140,16 +140,16 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(cp, ri, v, n, steps, threads):
+def cpu_sample(cp, ri, v, n, steps, threads, R=R_VEC):
     """Oracle recursion (plain path: one moment per step) on a bounded sample."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle as orc
 
-    kets = orc.random_phase_kets(n, R_VEC, 0)
+    kets = orc.random_phase_kets(n, R, 0)
     t0 = time.perf_counter()
     orc.cheb_moments(n, cp, ri, v, steps + 1, kets, kets, threads=threads, steps_limit=steps)
     dt = time.perf_counter() - t0
-    return n * R_VEC * steps / dt, dt
+    return n * R * steps / dt, dt
 
 
 def build_host_system():
@@ -638,6 +638,89 @@ def run_expand(args):
     return 0
 
 
+def run_small(args):
+    """Config-1 DoS (the reference's CPU-sized case): square 64 x 64 periodic,
+    t = 1, H~ = H / 4.05, M = 256, R = 8 random-phase vectors (seed 0), Jackson
+    kernel, rho on 1,024 energies in [-4, 4].  Launch/latency bound (a 512 KB
+    vector block): reports per-solve latency p50/p99 over --steps solves of the
+    resident plan (FP64 and mixed, doubling, graph replay on and off), the
+    drop-in C-ABI call with host buffers (H~ uploaded every call, as the
+    reference's cuSPARSE path does), and the CPU oracle on the whole solve."""
+    import torch
+
+    import tight_binding_gb300 as tb
+    from tight_binding_gb300 import capi
+
+    L, M, R, NE = 64, 256, 8, 1024
+    X = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (L, L))
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], float)
+    G = tb.GreenFunction(M, H, -4.05, 4.05)
+    Ht = G.scaled_HE
+    N = Ht.shape[0]
+    kets_h = tb.bases_of_uniform_ampl_with_random_phases(N, R, 0)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    kets_d = torch.from_numpy(np.ascontiguousarray(kets_h.T)).to(dev)
+    mu_d = torch.zeros(M, dtype=torch.float64, device=dev)
+    E = np.linspace(-4.0, 4.0, NE) / 4.05 * 0.999
+    steps = max(args.steps, 50)
+    out = {"small_dos": "square 64x64 PBC, t=1, a=4.05, M=256, R=8, Jackson, 1024 energies", "sites": N,
+           "solves": steps}
+    ref_mu = None
+    for name, prec, extra in (("fp64", "fp64", 0), ("fp64_no_graph", "fp64", capi.FLAG_NO_GRAPH),
+                              ("mixed", "mixed", 0), ("dd", "dd", 0)):
+        sol = tb.KpmSolver(Ht, R, precision=prec, doubling=True, flags=capi.FLAG_DEVICE_PTRS | extra)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * steps)]
+        for _ in range(args.warmup + 2):
+            with torch.cuda.stream(stream):
+                sol.run_device(M, kets_d.data_ptr(), kets_d.data_ptr(), mu_d.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+        for k in range(steps):
+            ev[2 * k].record(stream)
+            with torch.cuda.stream(stream):
+                sol.run_device(M, kets_d.data_ptr(), kets_d.data_ptr(), mu_d.data_ptr(), stream.cuda_stream)
+            ev[2 * k + 1].record(stream)
+        torch.cuda.synchronize()
+        lat = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(steps)]
+        mu = mu_d.cpu().numpy()
+        if ref_mu is None:
+            ref_mu = mu.copy()
+        out[name] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                     "updates_per_s": N * M * R / (float(np.percentile(lat, 50)) / 1e3),
+                     "rel_err_vs_fp64": float(np.max(np.abs(mu - ref_mu)) / abs(ref_mu[0]))}
+        del sol
+    # drop-in C-ABI call with host buffers (upload of H~ and kets, read-back of mu)
+    cp, ri, v = Ht.to_csc()
+    kets_c = np.asfortranarray(kets_h)
+    mu_h = np.zeros(M)
+    flags = capi.PREC_FP64 | capi.FLAG_DOUBLING
+
+    def dropin():
+        capi.check(capi.lib().tbk_cheb_braket_real(N, len(ri), capi.ptr(cp), capi.ptr(ri), capi.ptr(v), M,
+                                                   capi.ptr(kets_c), capi.ptr(kets_c), R, flags, capi.ptr(mu_h)))
+
+    for _ in range(args.warmup):
+        dropin()
+    t = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        dropin()
+        t.append((time.perf_counter() - t0) * 1e3)
+    out["dropin_e2e"] = {"p50_ms": float(np.percentile(t, 50)), "p99_ms": float(np.percentile(t, 99)),
+                         "rel_err_vs_fp64": float(np.max(np.abs(mu_h - ref_mu)) / abs(ref_mu[0]))}
+    # reconstruction of rho on the 1,024 energies
+    t0 = time.perf_counter()
+    rho = tb.dos_from_moments(ref_mu, tb.Jackson(), R, E)
+    out["rho_ms"] = (time.perf_counter() - t0) * 1e3
+    out["rho_integral"] = float(np.trapezoid(rho, E)) if hasattr(np, "trapezoid") else None
+    # CPU oracle on the whole solve (plain path, one moment per step)
+    for threads in (1, os.cpu_count() or 1):
+        rate, dt = cpu_sample(cp, ri, v, N, M - 1, threads, R)
+        out[f"cpu_oracle_{threads}t"] = {"ms": dt * 1e3, "updates_per_s": rate}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_kernel_only(args):
     """Small case of the same kernel for ncu captures: one mixed-precision DoS
     solve (doubling) on a honeycomb of --cells^2 cells, R = 32."""
@@ -696,7 +779,10 @@ def main():
                     help="mu_nm GEMM alone on random M x K complex blocks (profiling case)")
     ap.add_argument("--expand", type=float, default=None, metavar="T",
                     help="time evolution exp(-iHt) of 8 vectors to time T (vector-expansion leg)")
+    ap.add_argument("--small", action="store_true", help="config-1 DoS (square 64x64): latency-bound case")
     args = ap.parse_args()
+    if args.small:
+        return run_small(args)
     if args.expand is not None:
         return run_expand(args)
     if args.gemm:

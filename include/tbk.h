@@ -59,10 +59,13 @@ enum {
   TBK_FLAG_DEVICE_PTRS = 1 << 5,  /* bras/kets/mu are device pointers           */
   TBK_FLAG_NO_L2_ZIGZAG = 1 << 6, /* keep every step's sweep ascending          */
   TBK_FLAG_STAGED = 1 << 7,       /* TMA-staged warp-specialised step kernel      */
-  TBK_FLAG_TWO_STEP = 1 << 8      /* mixed doubling: two recursion steps per pass
+  TBK_FLAG_TWO_STEP = 1 << 8,     /* mixed doubling: two recursion steps per pass
                                      over memory (temporal blocking; 1/3 less DRAM
                                      traffic, but the gathers are latency-bound on
                                      GB300 and it measures slower, so opt-in)     */
+  TBK_FLAG_NO_GRAPH = 1 << 9      /* never replay the recursion as a CUDA graph
+                                     (small single-chunk plans capture their
+                                     launch sequence on the second identical run) */
 };
 
 /* =========================================================================

@@ -218,3 +218,26 @@ def test_two_step_passes_match_single_steps(gpu):
     ref = orc.cheb_moments(n, cp, ri, v, 130, kets, kets)
     mu = tb.KpmSolver(Ht, 32, precision="mixed", doubling=True, flags=two).run_random(130, 5)
     assert _err(mu, ref) <= MIXED_TOL, _err(mu, ref)
+
+
+@pytest.mark.parametrize("precision,doubling", [("fp64", True), ("fp64", False), ("mixed", True), ("dd", True)])
+def test_graph_replay_matches_direct_launches(gpu, precision, doubling):
+    """Small single-chunk plans capture their recursion on the second identical
+    run and replay it after: every run gives the bits of a plan that never
+    captures, also when the moment count changes between runs."""
+    tb = gpu
+    from tight_binding_gb300 import capi
+
+    _, H = _system(tb, "square", (64, 64), disorder=(1.0, 3))
+    G, cp, ri, v = _rescaled_csc(tb, H, 4.6)
+    kets = tb.bases_of_uniform_ampl_with_random_phases(64 * 64, 8, 0)
+    bras = kets if doubling else tb.bases_of_uniform_ampl_with_random_phases(64 * 64, 8, 1)
+    g = tb.KpmSolver(G.scaled_HE, 8, precision=precision, doubling=doubling)
+    d = tb.KpmSolver(G.scaled_HE, 8, precision=precision, doubling=doubling, flags=capi.FLAG_NO_GRAPH)
+    for M in (256, 256, 256, 256, 100, 100, 100, 256):
+        a = g.run(M, bras, kets)
+        b = d.run(M, bras, kets)
+        assert np.array_equal(a, b), M
+    ref = orc.cheb_moments(64 * 64, cp, ri, v, 256, bras, kets)
+    tol = {"fp64": 1e-10, "dd": DD_TOL, "mixed": MIXED_TOL}[precision]
+    assert np.max(np.abs(a - ref)) / abs(ref[0]) <= tol

@@ -31,6 +31,7 @@ FLAG_DEVICE_PTRS = 1 << 5
 FLAG_NO_L2_ZIGZAG = 1 << 6
 FLAG_STAGED = 1 << 7
 FLAG_TWO_STEP = 1 << 8
+FLAG_NO_GRAPH = 1 << 9
 
 BUILD_SPARSE = 0
 BUILD_PERIODIC_BARE = 1

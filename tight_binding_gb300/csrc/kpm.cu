@@ -503,7 +503,24 @@ struct tbk_kpm_s {
   bool fused = false;
   int32_t lag = 0, n_def = 0, n_waves = 0, tpt = 4, n_tasks = 0;
   DevBuf dep, isdef, deflist, wave;
+  // launch-bound plans (one chunk, small blocks): the recursion's launch
+  // sequence is captured once per (steps, mode, buffers) and replayed
+  cudaStream_t cap_st = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  struct GraphKey {
+    int32_t n_steps = -1;
+    bool braket = false;
+    const void *va = nullptr, *vb = nullptr, *part = nullptr, *bras = nullptr;
+    bool operator==(const GraphKey& o) const {
+      return n_steps == o.n_steps && braket == o.braket && va == o.va && vb == o.vb && part == o.part &&
+             bras == o.bras;
+    }
+  } gkey, seen;
 };
+
+// single-chunk plans whose work blocks fit in 64 MiB are launch-bound: replay
+// their recursion as a graph
+constexpr size_t kGraphBlockBytes = 64u << 20;
 
 static int plan_partials(tbk_kpm_s* P, int32_t n_steps) {
   if (n_steps <= P->cap_steps) return TBK_OK;
@@ -655,7 +672,8 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
         ++launches;
       }
     }
-    for (; s < n_steps; ++s) {
+    auto issue = [&](cudaStream_t q, int32_t s_begin, void* xx, void* yy) -> int {
+    for (int32_t s = s_begin; s < n_steps; ++s) {
       StepArgs a;
       a.n = (int32_t)P->n;
       a.n_tiles = tma ? P->tiles_tma : P->n_tiles;
@@ -666,9 +684,9 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
       a.ecol = E.col.as<int32_t>();
       a.eval = ell_vals(E, P->prec);
       a.diag = ell_diag(E, P->prec);
-      a.x = x;
-      a.y = y;
-      a.pv = y;
+      a.x = xx;
+      a.y = yy;
+      a.pv = yy;
       a.bras = braket ? P->bras.p : nullptr;
       a.part = P->part.as<double>() + (((int64_t)ch * n_steps + s) * 2) * G;
       const bool last_dot = doubling && s == n_steps - 1 && s > 0;   // dots only, no product
@@ -678,21 +696,69 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
       const bool first = s == 0;
       int rc;
       if (tma) {
-        if (mixed) rc = cplx ? launch_tma<float, true>(P->Rc, a, lay, first, braket, G, st)
-                             : launch_tma<float, false>(P->Rc, a, lay, first, braket, G, st);
-        else rc = cplx ? launch_tma<double, true>(P->Rc, a, lay, first, braket, G, st)
-                       : launch_tma<double, false>(P->Rc, a, lay, first, braket, G, st);
+        if (mixed) rc = cplx ? launch_tma<float, true>(P->Rc, a, lay, first, braket, G, q)
+                             : launch_tma<float, false>(P->Rc, a, lay, first, braket, G, q);
+        else rc = cplx ? launch_tma<double, true>(P->Rc, a, lay, first, braket, G, q)
+                       : launch_tma<double, false>(P->Rc, a, lay, first, braket, G, q);
       } else {
-        if (mixed) rc = cplx ? launch_step<float, true>(P->Rc, a, first, braket, G, st)
-                             : launch_step<float, false>(P->Rc, a, first, braket, G, st);
-        else if (P->prec == TBK_PREC_DD) rc = cplx ? launch_step<dd, true>(P->Rc, a, first, braket, G, st)
-                                                   : launch_step<dd, false>(P->Rc, a, first, braket, G, st);
-        else rc = cplx ? launch_step<double, true>(P->Rc, a, first, braket, G, st)
-                       : launch_step<double, false>(P->Rc, a, first, braket, G, st);
+        if (mixed) rc = cplx ? launch_step<float, true>(P->Rc, a, first, braket, G, q)
+                             : launch_step<float, false>(P->Rc, a, first, braket, G, q);
+        else if (P->prec == TBK_PREC_DD) rc = cplx ? launch_step<dd, true>(P->Rc, a, first, braket, G, q)
+                                                   : launch_step<dd, false>(P->Rc, a, first, braket, G, q);
+        else rc = cplx ? launch_step<double, true>(P->Rc, a, first, braket, G, q)
+                       : launch_step<double, false>(P->Rc, a, first, braket, G, q);
       }
       if (rc != TBK_OK) return rc;
-      ++launches;
-      std::swap(x, y);   // y now holds v_{n+1}; it becomes x, x (v_n) becomes the next v_{n-1}
+      std::swap(xx, yy);   // yy now holds v_{n+1}; it becomes xx, xx (v_n) becomes the next v_{n-1}
+    }
+    return TBK_OK;
+    };
+    const bool graphable = P->n_chunks == 1 && s == 0 && !tma && !(P->flags & TBK_FLAG_NO_GRAPH) &&
+                           P->va.bytes <= kGraphBlockBytes;
+    if (graphable) {
+      tbk_kpm_s::GraphKey key;
+      key.n_steps = n_steps;
+      key.braket = braket;
+      key.va = P->va.p;
+      key.vb = P->vb.p;
+      key.part = P->part.p;
+      key.bras = braket ? P->bras.p : nullptr;
+      if (!(P->gexec && P->gkey == key) && P->seen == key) {
+        // second identical run: capture the launch sequence on the plan's own
+        // stream (thread-local mode: other threads' launches are unaffected)
+        if (!P->cap_st) TBK_CUDA(cudaStreamCreateWithFlags(&P->cap_st, cudaStreamNonBlocking));
+        if (P->gexec) {
+          cudaGraphExecDestroy(P->gexec);
+          P->gexec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        TBK_CUDA(cudaStreamBeginCapture(P->cap_st, cudaStreamCaptureModeThreadLocal));
+        const int rc = issue(P->cap_st, 0, x, y);
+        const cudaError_t ec = cudaStreamEndCapture(P->cap_st, &g);
+        if (rc != TBK_OK) {
+          if (g) cudaGraphDestroy(g);
+          return rc;
+        }
+        if (ec != cudaSuccess) return fail(TBK_ERR_CUDA, "recursion graph capture: %s", cudaGetErrorString(ec));
+        const cudaError_t ei = cudaGraphInstantiate(&P->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ei != cudaSuccess) {
+          P->gexec = nullptr;
+          return fail(TBK_ERR_CUDA, "recursion graph instantiate: %s", cudaGetErrorString(ei));
+        }
+        P->gkey = key;
+      }
+      P->seen = key;
+      if (P->gexec && P->gkey == key) {
+        TBK_CUDA(cudaGraphLaunch(P->gexec, st));
+        launches += n_steps;
+      } else {
+        TBK_TRY(issue(st, 0, x, y));
+        launches += n_steps;
+      }
+    } else {
+      TBK_TRY(issue(st, s, x, y));
+      launches += n_steps - s;
     }
     TBK_CUDA(cudaEventRecord(P->ev1, st));
     TBK_CUDA(cudaEventSynchronize(P->ev1));
@@ -845,6 +911,8 @@ void tbk_kpm_destroy(tbk_kpm P) {
   cudaDeviceSynchronize();
   if (P->ev0) cudaEventDestroy(P->ev0);
   if (P->ev1) cudaEventDestroy(P->ev1);
+  if (P->gexec) cudaGraphExecDestroy(P->gexec);
+  if (P->cap_st) cudaStreamDestroy(P->cap_st);
   delete P;
 }
 
