@@ -627,8 +627,8 @@ def run_expand(args):
     t0 = time.perf_counter()
     out = tb.cheb_expand(G.scaled_HE, coef, kets, args.precision)
     dt = time.perf_counter() - t0
-    csz = {"mixed": 8, "fp64": 16, "dd": 32}[args.precision]
-    vsz = {"mixed": 4, "fp64": 8, "dd": 16}[args.precision]
+    csz = {"mixed": 8, "fp64": 16, "dd": 16}[args.precision]      # complex element: c64, c128, 2 x (hi, lo) float
+    vsz = {"mixed": 4, "fp64": 8, "dd": 8}[args.precision]        # real matrix value
     nnz_off = 3 * n
     per_term = nnz_off * (4 + vsz) + n * vsz + n * R * (3 * csz + csz + 32)
     print(json.dumps({"expand": "exp(-iHt)", "t": args.expand, "terms": len(coef), "sites": n, "R": R,
@@ -643,7 +643,8 @@ def run_small(args):
     t = 1, H~ = H / 4.05, M = 256, R = 8 random-phase vectors (seed 0), Jackson
     kernel, rho on 1,024 energies in [-4, 4].  Launch/latency bound (a 512 KB
     vector block): reports per-solve latency p50/p99 over --steps solves of the
-    resident plan (FP64 and mixed, doubling, graph replay on and off), the
+    resident plan (FP64, mixed and double-float, doubling; the one-launch
+    recursion against per-step launches with and without graph replay), the
     drop-in C-ABI call with host buffers (H~ uploaded every call, as the
     reference's cuSPARSE path does), and the CPU oracle on the whole solve."""
     import torch
@@ -667,7 +668,8 @@ def run_small(args):
     out = {"small_dos": "square 64x64 PBC, t=1, a=4.05, M=256, R=8, Jackson, 1024 energies", "sites": N,
            "solves": steps}
     ref_mu = None
-    for name, prec, extra in (("fp64", "fp64", 0), ("fp64_no_graph", "fp64", capi.FLAG_NO_GRAPH),
+    for name, prec, extra in (("fp64", "fp64", 0), ("fp64_per_step_graph", "fp64", capi.FLAG_NO_PERSISTENT),
+                              ("fp64_per_step_launches", "fp64", capi.FLAG_NO_PERSISTENT | capi.FLAG_NO_GRAPH),
                               ("mixed", "mixed", 0), ("dd", "dd", 0)):
         sol = tb.KpmSolver(Ht, R, precision=prec, doubling=True, flags=capi.FLAG_DEVICE_PTRS | extra)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * steps)]

@@ -63,9 +63,14 @@ enum {
                                      over memory (temporal blocking; 1/3 less DRAM
                                      traffic, but the gathers are latency-bound on
                                      GB300 and it measures slower, so opt-in)     */
-  TBK_FLAG_NO_GRAPH = 1 << 9      /* never replay the recursion as a CUDA graph
+  TBK_FLAG_NO_GRAPH = 1 << 9,     /* never replay the recursion as a CUDA graph
                                      (small single-chunk plans capture their
                                      launch sequence on the second identical run) */
+  TBK_FLAG_NO_PERSISTENT = 1 << 10 /* one launch per recursion step even when the
+                                     two work vectors of a random vector fit in
+                                     shared memory (by default such plans run the
+                                     whole recursion in one launch, one CTA per
+                                     random vector)                             */
 };
 
 /* =========================================================================

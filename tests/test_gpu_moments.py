@@ -232,8 +232,9 @@ def test_graph_replay_matches_direct_launches(gpu, precision, doubling):
     G, cp, ri, v = _rescaled_csc(tb, H, 4.6)
     kets = tb.bases_of_uniform_ampl_with_random_phases(64 * 64, 8, 0)
     bras = kets if doubling else tb.bases_of_uniform_ampl_with_random_phases(64 * 64, 8, 1)
-    g = tb.KpmSolver(G.scaled_HE, 8, precision=precision, doubling=doubling)
-    d = tb.KpmSolver(G.scaled_HE, 8, precision=precision, doubling=doubling, flags=capi.FLAG_NO_GRAPH)
+    multi = capi.FLAG_NO_PERSISTENT
+    g = tb.KpmSolver(G.scaled_HE, 8, precision=precision, doubling=doubling, flags=multi)
+    d = tb.KpmSolver(G.scaled_HE, 8, precision=precision, doubling=doubling, flags=multi | capi.FLAG_NO_GRAPH)
     for M in (256, 256, 256, 256, 100, 100, 100, 256):
         a = g.run(M, bras, kets)
         b = d.run(M, bras, kets)
@@ -241,3 +242,31 @@ def test_graph_replay_matches_direct_launches(gpu, precision, doubling):
     ref = orc.cheb_moments(64 * 64, cp, ri, v, 256, bras, kets)
     tol = {"fp64": 1e-10, "dd": DD_TOL, "mixed": MIXED_TOL}[precision]
     assert np.max(np.abs(a - ref)) / abs(ref[0]) <= tol
+
+
+@pytest.mark.parametrize("precision,doubling,cplx,R", [("fp64", True, False, 8), ("fp64", False, True, 3),
+                                                       ("mixed", True, True, 8), ("mixed", False, False, 5),
+                                                       ("dd", True, False, 4), ("dd", False, True, 2)])
+def test_one_launch_recursion_matches_oracle(gpu, precision, doubling, cplx, R):
+    """Plans whose two work vectors per random vector fit in shared memory run
+    the whole recursion in one launch (one CTA per vector): moments against the
+    oracle and against the one-launch-per-step path."""
+    tb = gpu
+    from tight_binding_gb300 import capi
+
+    gauge = landau_gauge(0.05) if cplx else None
+    _, H = _system(tb, "honeycomb", (40, 36), cplx=cplx, disorder=(1.0, 5), gauge=gauge)
+    G, cp, ri, v = _rescaled_csc(tb, H, 8.8)
+    n = H.shape[0]
+    kets = tb.bases_of_uniform_ampl_with_random_phases(n, R, 2)
+    bras = kets if doubling else tb.bases_of_uniform_ampl_with_random_phases(n, R, 3)
+    one = tb.KpmSolver(G.scaled_HE, R, precision=precision, doubling=doubling)
+    multi = tb.KpmSolver(G.scaled_HE, R, precision=precision, doubling=doubling, flags=capi.FLAG_NO_PERSISTENT)
+    M = 300
+    a = one.run(M, bras, kets)
+    assert one.last_timing()[1] == 1                     # one recursion launch
+    b = multi.run(M, bras, kets)
+    ref = orc.cheb_moments(n, cp, ri, v, M, bras, kets)
+    tol = {"fp64": 1e-10, "dd": DD_TOL, "mixed": MIXED_TOL}[precision]
+    assert np.max(np.abs(a - ref)) / abs(ref[0]) <= tol
+    assert np.max(np.abs(a - b)) / abs(ref[0]) <= (1e-13 if precision != "mixed" else 1e-6)

@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
 }  // namespace tbk
 #include "kpm_tma.cuh"
 #include "kpm_fused.cuh"
+#include "kpm_small.cuh"
 namespace tbk {
 
 // Column-major complex128 (Eigen) -> site-major work block of width Rp.
@@ -630,6 +631,42 @@ static int launch_fused(tbk_kpm_s* P, void* A, void* B, double* part1, double* p
   return TBK_OK;
 }
 
+// one-launch recursion (kpm_small.cuh) when a random vector's two work vectors
+// fit in shared memory
+constexpr size_t kSmallSmemBytes = 200u << 10;
+
+static bool small_eligible(const tbk_kpm_s* P, bool tma) {
+  return P->n_chunks == 1 && !tma && !(P->flags & (TBK_FLAG_NO_PERSISTENT | TBK_FLAG_TWO_STEP)) &&
+         2 * (size_t)P->n_pad * P->csize <= kSmallSmemBytes && P->R <= P->grid_max;
+}
+
+template <typename F, bool CPLX_H>
+static int launch_small_t(tbk_kpm_s* P, bool braket, int32_t n_steps, cudaStream_t st) {
+  using CT = typename C2<F>::T;
+  const EllDev& E = P->H->ell;
+  const int smem = (int)(2 * (size_t)P->n_pad * sizeof(CT));
+  auto kern = braket ? kpm_small_kernel<F, CPLX_H, true> : kpm_small_kernel<F, CPLX_H, false>;
+  TBK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  kern<<<P->R, kSmallThreads, smem, st>>>((int32_t)P->n, (int32_t)P->n_pad, n_steps, P->Rc,
+                                           E.slice_off.as<int32_t>(), E.col.as<int32_t>(),
+                                           static_cast<const F*>(ell_vals(E, P->prec)),
+                                           static_cast<const F*>(ell_diag(E, P->prec)),
+                                           static_cast<const CT*>(P->va.p),
+                                           braket ? static_cast<const CT*>(P->bras.p) : nullptr,
+                                           P->part.as<double>(), P->R);
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
+}
+
+static int launch_small(tbk_kpm_s* P, bool braket, int32_t n_steps, cudaStream_t st) {
+  const bool c = P->H->ell.cplx != 0;
+  if (P->prec == TBK_PREC_FP64) return c ? launch_small_t<double, true>(P, braket, n_steps, st)
+                                         : launch_small_t<double, false>(P, braket, n_steps, st);
+  if (P->prec == TBK_PREC_DD) return c ? launch_small_t<dd, true>(P, braket, n_steps, st)
+                                       : launch_small_t<dd, false>(P, braket, n_steps, st);
+  return c ? launch_small_t<float, true>(P, braket, n_steps, st) : launch_small_t<float, false>(P, braket, n_steps, st);
+}
+
 // Runs all chunks.  kets_loader(r0, dst) fills the chunk's v0 (site-major);
 // bras_loader(r0, dst) fills the chunk's bras block (braket mode only).
 template <typename KL, typename BL>
@@ -654,6 +691,8 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
   const bool cplx = P->H->ell.cplx != 0;
   float ms_total = 0.f;
   int32_t launches = 0;
+  const bool small = small_eligible(P, tma);
+  const int32_t nblk = small ? P->R : G;       // partials per (step, slot)
   for (int32_t ch = 0; ch < P->n_chunks; ++ch) {
     const int32_t r0 = ch * P->Rc;
     TBK_TRY(kets_loader(r0, P->va.p));
@@ -715,7 +754,10 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
     };
     const bool graphable = P->n_chunks == 1 && s == 0 && !tma && !(P->flags & TBK_FLAG_NO_GRAPH) &&
                            P->va.bytes <= kGraphBlockBytes;
-    if (graphable) {
+    if (small) {
+      TBK_TRY(launch_small(P, braket, n_steps, st));
+      launches += 1;
+    } else if (graphable) {
       tbk_kpm_s::GraphKey key;
       key.n_steps = n_steps;
       key.braket = braket;
@@ -766,7 +808,7 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
     TBK_CUDA(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
     ms_total += ms;
   }
-  reduce_partials_kernel<<<dim3(n_steps, 2), 256, 0, st>>>(P->part.as<double>(), P->n_chunks, n_steps, G,
+  reduce_partials_kernel<<<dim3(n_steps, 2), 256, 0, st>>>(P->part.as<double>(), P->n_chunks, n_steps, nblk,
                                                           P->sums.as<double>());
   TBK_CHECK_LAUNCH();
   assemble_moments_kernel<<<(n_mom + 255) / 256, 256, 0, st>>>(P->sums.as<double>(), n_mom, doubling ? 1 : 0,
