@@ -140,6 +140,11 @@ def test_resident_plan_is_deterministic_and_random_kets(gpu):
     f = tb.KpmSolver(G.scaled_HE, 16, precision="fp64", doubling=True)
     assert _err(f.run_random(128, 5), ref) <= 1e-10
     ms, launches, bytes_ = s.last_timing()
+    assert launches == 1 and ms > 0 and bytes_ > 0        # 2,048 sites: one-launch recursion
+    from tight_binding_gb300 import capi
+    m = tb.KpmSolver(G.scaled_HE, 16, precision="mixed", doubling=True, flags=capi.FLAG_NO_PERSISTENT)
+    assert _err(m.run_random(128, 5), ref) <= MIXED_TOL
+    ms, launches, bytes_ = m.last_timing()
     assert launches == 65 and ms > 0 and bytes_ > 0
 
 
