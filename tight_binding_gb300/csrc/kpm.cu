@@ -517,6 +517,8 @@ struct tbk_kpm_s {
              bras == o.bras;
     }
   } gkey, seen;
+  int small_state = 0;              // one-launch recursion: 0 undecided, 1 used, -1 not applicable
+  SmallLayout slay{};
 };
 
 // single-chunk plans whose work blocks fit in 64 MiB are launch-bound: replay
@@ -631,30 +633,111 @@ static int launch_fused(tbk_kpm_s* P, void* A, void* B, double* part1, double* p
   return TBK_OK;
 }
 
-// one-launch recursion (kpm_small.cuh) when a random vector's two work vectors
-// fit in shared memory
-constexpr size_t kSmallSmemBytes = 200u << 10;
+// one-launch recursion (kpm_small.cuh): one thread-block cluster per random
+// vector keeps the vector and its slice of H~ in shared memory
+constexpr int32_t kSmallSmemBytes = 200 << 10;
 
-static bool small_eligible(const tbk_kpm_s* P, bool tma) {
-  return P->n_chunks == 1 && !tma && !(P->flags & (TBK_FLAG_NO_PERSISTENT | TBK_FLAG_TWO_STEP)) &&
-         2 * (size_t)P->n_pad * P->csize <= kSmallSmemBytes && P->R <= P->grid_max;
+template <typename F, bool CPLX_H>
+static void* small_kernel_ptr(bool braket) {
+  return braket ? reinterpret_cast<void*>(kpm_cluster_kernel<F, CPLX_H, true>)
+                : reinterpret_cast<void*>(kpm_cluster_kernel<F, CPLX_H, false>);
+}
+static void* small_kernel(int prec, bool cplx, bool braket) {
+  if (prec == TBK_PREC_FP64) return cplx ? small_kernel_ptr<double, true>(braket) : small_kernel_ptr<double, false>(braket);
+  if (prec == TBK_PREC_DD) return cplx ? small_kernel_ptr<dd, true>(braket) : small_kernel_ptr<dd, false>(braket);
+  return cplx ? small_kernel_ptr<float, true>(braket) : small_kernel_ptr<float, false>(braket);
+}
+
+// decides once per plan whether the one-launch recursion applies and lays out
+// its shared memory: rows per CTA a power of two >= 32, at most 8 CTAs per
+// cluster, at most 2 rows per thread
+static int plan_small(tbk_kpm_s* P, bool tma) {
+  if (P->small_state != 0) return TBK_OK;
+  P->small_state = -1;
+  if (P->n_chunks != 1 || tma || (P->flags & (TBK_FLAG_NO_PERSISTENT | TBK_FLAG_TWO_STEP))) return TBK_OK;
+  const EllDev& E = P->H->ell;
+  const int32_t n = (int32_t)P->n;
+  int32_t rpc = 32, lg = 5;
+  while ((int64_t)rpc * kClusterMax < n) { rpc <<= 1; ++lg; }
+  if (rpc > 2 * kSmallThreadsMax) return TBK_OK;
+  SmallLayout L;
+  L.rpc = rpc;
+  L.lg_rpc = lg;
+  L.cs = (n + rpc - 1) / rpc;
+  L.threads = std::min(rpc, kSmallThreadsMax);
+  const bool cplx = E.cplx != 0;
+  const int fb = P->prec == TBK_PREC_MIXED ? 4 : 8;      // float, double, dd (hi, lo)
+  L.vb = fb * (cplx ? 2 : 1);
+  L.csz = (int32_t)P->csize;
+  std::vector<int32_t> so((size_t)E.n_slices + 1);
+  TBK_CUDA(cudaMemcpy(so.data(), E.slice_off.p, sizeof(int32_t) * so.size(), cudaMemcpyDeviceToHost));
+  int32_t max_ne = 0;
+  for (int q = 0; q < L.cs; ++q) {
+    const int32_t a = std::min(q * (rpc >> 5), E.n_slices), b = std::min((q + 1) * (rpc >> 5), E.n_slices);
+    max_ne = std::max(max_ne, so[b] - so[a]);
+  }
+  L.max_ne = max_ne;
+  if (L.bytes() > kSmallSmemBytes) return TBK_OK;
+  void* fn[2] = {small_kernel(P->prec, cplx, false), small_kernel(P->prec, cplx, true)};
+  for (void* f : fn) {
+    TBK_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, L.bytes()));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = L.cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(P->R * L.cs);
+    cfg.blockDim = dim3(L.threads);
+    cfg.dynamicSmemBytes = L.bytes();
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, f, &cfg) != cudaSuccess || clusters < 1) {
+      cudaGetLastError();
+      return TBK_OK;
+    }
+  }
+  P->slay = L;
+  P->small_state = 1;
+  if (P->R * L.cs > P->grid_max) {         // partials: one pair per CTA and step
+    P->grid_max = P->R * L.cs;
+    P->cap_steps = 0;
+  }
+  return TBK_OK;
 }
 
 template <typename F, bool CPLX_H>
 static int launch_small_t(tbk_kpm_s* P, bool braket, int32_t n_steps, cudaStream_t st) {
   using CT = typename C2<F>::T;
   const EllDev& E = P->H->ell;
-  const int smem = (int)(2 * (size_t)P->n_pad * sizeof(CT));
-  auto kern = braket ? kpm_small_kernel<F, CPLX_H, true> : kpm_small_kernel<F, CPLX_H, false>;
-  TBK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  kern<<<P->R, kSmallThreads, smem, st>>>((int32_t)P->n, (int32_t)P->n_pad, n_steps, P->Rc,
-                                           E.slice_off.as<int32_t>(), E.col.as<int32_t>(),
-                                           static_cast<const F*>(ell_vals(E, P->prec)),
-                                           static_cast<const F*>(ell_diag(E, P->prec)),
-                                           static_cast<const CT*>(P->va.p),
-                                           braket ? static_cast<const CT*>(P->bras.p) : nullptr,
-                                           P->part.as<double>(), P->R);
-  TBK_CHECK_LAUNCH();
+  const SmallLayout L = P->slay;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = L.cs;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(P->R * L.cs);
+  cfg.blockDim = dim3(L.threads);
+  cfg.dynamicSmemBytes = L.bytes();
+  cfg.stream = st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const int32_t n = (int32_t)P->n;
+  const int32_t* so = E.slice_off.as<int32_t>();
+  const int32_t* co = E.col.as<int32_t>();
+  const F* ev = static_cast<const F*>(ell_vals(E, P->prec));
+  const F* dg = static_cast<const F*>(ell_diag(E, P->prec));
+  const CT* k = static_cast<const CT*>(P->va.p);
+  const CT* b = braket ? static_cast<const CT*>(P->bras.p) : nullptr;
+  double* pt = P->part.as<double>();
+  if (braket)
+    TBK_CUDA(cudaLaunchKernelEx(&cfg, kpm_cluster_kernel<F, CPLX_H, true>, n, E.n_slices, n_steps, P->Rc, L, so, co,
+                                ev, dg, k, b, pt));
+  else
+    TBK_CUDA(cudaLaunchKernelEx(&cfg, kpm_cluster_kernel<F, CPLX_H, false>, n, E.n_slices, n_steps, P->Rc, L, so, co,
+                                ev, dg, k, b, pt));
   return TBK_OK;
 }
 
@@ -676,6 +759,8 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
   const bool doubling = !braket;
   // doubling: step s yields mu_2s and mu_2s-1, so steps 0 .. n_mom/2 are needed
   const int32_t n_steps = doubling ? (n_mom <= 2 ? 1 : n_mom / 2 + 1) : n_mom - 1;
+  const bool tma = P->use_tma && (P->flags & TBK_FLAG_STAGED);
+  TBK_TRY(plan_small(P, tma));
   TBK_TRY(plan_partials(P, n_steps));
   TBK_TRY(plan_mu(P, n_mom));
   if (braket && P->bras.bytes < P->va.bytes) {
@@ -683,7 +768,6 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
     TBK_CUDA(cudaMemsetAsync(P->bras.p, 0, P->bras.bytes, st));
   }
   const EllDev& E = P->H->ell;
-  const bool tma = P->use_tma && (P->flags & TBK_FLAG_STAGED);
   const int G = tma ? (braket ? P->grid_brk : P->grid_dbl) : P->grid;
   const TmaLayout& lay = braket ? P->lay_brk : P->lay_dbl;
   TBK_CUDA(cudaMemsetAsync(P->err.p, 0, sizeof(int), st));
@@ -691,8 +775,8 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
   const bool cplx = P->H->ell.cplx != 0;
   float ms_total = 0.f;
   int32_t launches = 0;
-  const bool small = small_eligible(P, tma);
-  const int32_t nblk = small ? P->R : G;       // partials per (step, slot)
+  const bool small = P->small_state == 1;
+  const int32_t nblk = small ? P->R * P->slay.cs : G;    // partials per (step, slot)
   for (int32_t ch = 0; ch < P->n_chunks; ++ch) {
     const int32_t r0 = ch * P->Rc;
     TBK_TRY(kets_loader(r0, P->va.p));

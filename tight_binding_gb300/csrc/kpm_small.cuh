@@ -2,69 +2,133 @@
 //
 // A 4,096-site lattice with 8 vectors (the reference's CPU-sized case) moves
 // 512 KB per step: each step of the one-pass kernel is a few microseconds of
-// launch and tail, so the solve is launch-bound.  Here one CTA owns one random
-// vector for the whole solve: v_n and v_{n-1} live in shared memory (the
-// recursion writes v_{n+1} over v_{n-1} in place), H~ is read through the
-// read-only path (L1/L2-resident), and a __syncthreads separates the steps.
+// launch, gather latency and tail, so the solve is latency-bound.  Here one
+// thread-block cluster owns one random vector for the whole solve.  The
+// cluster's CTAs split the rows (rpc rows each, a power of two and a multiple
+// of the 32-row ELL slices); each CTA keeps its rows of v_n and v_{n-1} and its
+// slice of H~ (ELL columns, values, diagonal) in shared memory, reads
+// neighbours owned by other CTAs through distributed shared memory, writes
+// v_{n+1} over its v_{n-1} in place, and one cluster barrier separates the
+// steps.  Nothing goes to DRAM between steps except two FP64 partials per CTA.
 // Every row is computed with the same operations in the same order as the
-// one-pass kernel (diagonal first, then the ELL entries), so the vectors are
-// bit-identical to it; only the moment sums are grouped differently (per-warp
-// FP64 sums, then the CTA's warps in a fixed order, per step and vector).
+// one-pass kernel (diagonal first, then the ELL entries), so the vectors take
+// the same values; only the moment sums are grouped differently.
 //
-// Partials: part[(step * 2 + slot) * nblk + vector], the layout the fixed-order
+// Partials: part[(step * 2 + slot) * nblk + CTA], the layout the fixed-order
 // reduction of the multi-launch path reads (one chunk).
 #pragma once
+#include <cooperative_groups.h>
 
 namespace tbk {
 
-constexpr int kSmallThreads = 1024;
+constexpr int kClusterMax = 8;          // portable cluster size
+constexpr int kSmallThreadsMax = 1024;
+
+// shared-memory layout of one CTA (bytes), shared by host and device
+struct SmallLayout {
+  int32_t rpc, lg_rpc, cs, threads;     // rows per CTA (2^lg_rpc), cluster size, threads per CTA
+  int32_t max_ne;                       // largest ELL entry count of a CTA's slices
+  int32_t vb;                           // bytes of one matrix value (F, or 2 F for complex H)
+  int32_t csz;                          // bytes of one complex vector element
+  __host__ __device__ int32_t off_x() const { return 0; }
+  __host__ __device__ int32_t off_diag() const { return 2 * rpc * csz; }
+  __host__ __device__ int32_t off_soff() const { return off_diag() + rpc * vb; }
+  __host__ __device__ int32_t off_cols() const { return off_soff() + ((rpc / 32 + 1) * 4 + 15) / 16 * 16; }
+  __host__ __device__ int32_t off_vals() const { return off_cols() + (max_ne * 4 + 15) / 16 * 16; }
+  __host__ __device__ int32_t bytes() const { return off_vals() + (max_ne * vb + 15) / 16 * 16; }
+};
 
 template <typename F, bool CPLX_H, bool BRAKET>
-__global__ void __launch_bounds__(kSmallThreads) kpm_small_kernel(
-    int32_t n, int32_t n_pad, int32_t n_steps, int32_t Rp, const int32_t* __restrict__ soff,
+__global__ void __launch_bounds__(kSmallThreadsMax) kpm_cluster_kernel(
+    int32_t n, int32_t n_slices, int32_t n_steps, int32_t Rp, SmallLayout L, const int32_t* __restrict__ soff,
     const int32_t* __restrict__ ecol, const F* __restrict__ eval, const F* __restrict__ diag,
     const typename C2<F>::T* __restrict__ kets, const typename C2<F>::T* __restrict__ bras,
-    double* __restrict__ part, int32_t nblk) {
+    double* __restrict__ part) {
+  namespace cg = cooperative_groups;
   using CT = typename C2<F>::T;
-  extern __shared__ __align__(16) unsigned char small_smem[];
-  CT* va = reinterpret_cast<CT*>(small_smem);
-  CT* vb = va + n_pad;
-  __shared__ double wsum[2][2][kSmallThreads / 32];
-  const int32_t r = blockIdx.x;                 // the vector this CTA owns
+  constexpr int VW = CPLX_H ? 2 : 1;    // F values per matrix value
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ double wsum[2][2][kSmallThreadsMax / 32];
+  cg::cluster_group cl = cg::this_cluster();
+  const int q = (int)cl.block_rank();
+  const int32_t vec = blockIdx.x / L.cs;             // the random vector this cluster owns
+  const int32_t row0 = q * L.rpc;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int32_t i = threadIdx.x; i < n_pad; i += blockDim.x) {
+  CT* xa = reinterpret_cast<CT*>(sm + L.off_x());
+  CT* xb = xa + L.rpc;
+  F* dg = reinterpret_cast<F*>(sm + L.off_diag());
+  int32_t* so = reinterpret_cast<int32_t*>(sm + L.off_soff());
+  int32_t* cols = reinterpret_cast<int32_t*>(sm + L.off_cols());
+  F* vals = reinterpret_cast<F*>(sm + L.off_vals());
+  // this CTA's slices of H~ and rows of the kets
+  const int32_t sl0 = min(row0 >> 5, n_slices);
+  const int32_t nsl = L.rpc >> 5;
+  const int32_t base = soff[sl0];
+  const int32_t ne = soff[min(sl0 + nsl, n_slices)] - base;
+  for (int32_t j = threadIdx.x; j <= nsl; j += blockDim.x) so[j] = soff[min(sl0 + j, n_slices)] - base;
+  for (int32_t e = threadIdx.x; e < ne; e += blockDim.x) {
+    cols[e] = ecol[base + e];
+#pragma unroll
+    for (int u = 0; u < VW; ++u) {
+      if constexpr (is_dd<F>) {
+        const float2 p = __ldg(reinterpret_cast<const float2*>(eval) + ((int64_t)base + e) * VW + u);
+        vals[e * VW + u] = dd(p.x, p.y);
+      } else {
+        vals[e * VW + u] = __ldg(eval + ((int64_t)base + e) * VW + u);
+      }
+    }
+  }
+  for (int32_t li = threadIdx.x; li < L.rpc; li += blockDim.x) {
+    const int32_t i = row0 + li;
     CT z;
     z.x = F(0);
     z.y = F(0);
-    va[i] = i < n ? kets[(int64_t)i * Rp + r] : z;
-    vb[i] = z;
+#pragma unroll
+    for (int u = 0; u < VW; ++u) {
+      if (i < n) {
+        if constexpr (is_dd<F>) {
+          const float2 p = __ldg(reinterpret_cast<const float2*>(diag) + (int64_t)i * VW + u);
+          dg[li * VW + u] = dd(p.x, p.y);
+        } else {
+          dg[li * VW + u] = __ldg(diag + (int64_t)i * VW + u);
+        }
+      } else {
+        dg[li * VW + u] = F(0);
+      }
+    }
+    xa[li] = i < n ? kets[(int64_t)i * Rp + vec] : z;
+    xb[li] = z;
   }
-  __syncthreads();
+  cl.sync();
   for (int32_t s = 0; s < n_steps; ++s) {
     const bool first = s == 0;
     const bool last_dot = !BRAKET && s == n_steps - 1 && s > 0;   // dots only, no product
-    const CT* x = (s & 1) ? vb : va;
-    CT* y = (s & 1) ? va : vb;                  // v_{s-1} on entry, v_{s+1} on exit
+    CT* x = (s & 1) ? xb : xa;
+    CT* y = (s & 1) ? xa : xb;                  // v_{s-1} on entry, v_{s+1} on exit
     double m0 = 0.0, m1 = 0.0;
-    for (int32_t i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int32_t li = threadIdx.x; li < L.rpc; li += blockDim.x) {
+      if (row0 + li >= n) continue;
       LaneV<F, 1> xs, prev, acc, out;
-      xs.re[0] = x[i].x;
-      xs.im[0] = x[i].y;
-      prev.re[0] = y[i].x;
-      prev.im[0] = y[i].y;
+      xs.re[0] = x[li].x;
+      xs.im[0] = x[li].y;
+      prev.re[0] = y[li].x;
+      prev.im[0] = y[li].y;
       if (!last_dot) {
         acc.re[0] = F(0);
         acc.im[0] = F(0);
-        HVal<F, CPLX_H>::load(diag, i).template fma<1>(xs, acc);
-        const int32_t sl = i >> 5, l = i & 31;
-        const int32_t off = soff[sl];
-        const int32_t w = (soff[sl + 1] - off) >> 5;
+        HVal<F, CPLX_H>::load_smem(dg, li).template fma<1>(xs, acc);
+        const int32_t l = li & 31;
+        const int32_t off = so[li >> 5];
+        const int32_t w = (so[(li >> 5) + 1] - off) >> 5;
         for (int32_t k = 0; k < w; ++k) {
-          const int32_t c = __ldg(ecol + off + l + (int64_t)k * 32);
+          const int32_t e = off + l + k * 32;
+          const int32_t c = cols[e];
+          const CT* xr = cl.map_shared_rank(x, (unsigned)(c >> L.lg_rpc));
+          const CT v = xr[c & (L.rpc - 1)];
           LaneV<F, 1> xv;
-          xv.re[0] = x[c].x;
-          xv.im[0] = x[c].y;
-          HVal<F, CPLX_H>::load(eval, off + l + (int64_t)k * 32).template fma<1>(xv, acc);
+          xv.re[0] = v.x;
+          xv.im[0] = v.y;
+          HVal<F, CPLX_H>::load_smem(vals, e).template fma<1>(xv, acc);
         }
         if (first) {
           out = acc;
@@ -76,7 +140,7 @@ __global__ void __launch_bounds__(kSmallThreads) kpm_small_kernel(
         out = prev;
       }
       if constexpr (BRAKET) {
-        const CT b = bras[(int64_t)i * Rp + r];
+        const CT b = bras[(int64_t)(row0 + li) * Rp + vec];
         m0 += static_cast<double>(b.x * out.re[0] + b.y * out.im[0]);
         if (first) m1 += static_cast<double>(b.x * xs.re[0] + b.y * xs.im[0]);
       } else {
@@ -88,7 +152,7 @@ __global__ void __launch_bounds__(kSmallThreads) kpm_small_kernel(
         CT o;
         o.x = out.re[0];
         o.y = out.im[0];
-        y[i] = o;
+        y[li] = o;
       }
     }
 #pragma unroll
@@ -100,15 +164,15 @@ __global__ void __launch_bounds__(kSmallThreads) kpm_small_kernel(
       wsum[s & 1][0][warp] = m0;
       wsum[s & 1][1][warp] = m1;
     }
-    __syncthreads();
+    cl.sync();                                   // step done everywhere: y becomes the next x
     if (threadIdx.x == 0) {
       double a = 0.0, b = 0.0;
-      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
-        a += wsum[s & 1][0][q];
-        b += wsum[s & 1][1][q];
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        a += wsum[s & 1][0][w];
+        b += wsum[s & 1][1][w];
       }
-      part[((int64_t)s * 2 + 0) * nblk + r] = a;
-      part[((int64_t)s * 2 + 1) * nblk + r] = b;
+      part[((int64_t)s * 2 + 0) * gridDim.x + blockIdx.x] = a;
+      part[((int64_t)s * 2 + 1) * gridDim.x + blockIdx.x] = b;
     }
   }
 }
