@@ -120,15 +120,28 @@ __global__ void __launch_bounds__(kSmallThreadsMax) kpm_cluster_kernel(
         const int32_t l = li & 31;
         const int32_t off = so[li >> 5];
         const int32_t w = (so[(li >> 5) + 1] - off) >> 5;
-        for (int32_t k = 0; k < w; ++k) {
-          const int32_t e = off + l + k * 32;
-          const int32_t c = cols[e];
-          const CT* xr = cl.map_shared_rank(x, (unsigned)(c >> L.lg_rpc));
-          const CT v = xr[c & (L.rpc - 1)];
-          LaneV<F, 1> xv;
-          xv.re[0] = v.x;
-          xv.im[0] = v.y;
-          HVal<F, CPLX_H>::load_smem(vals, e).template fma<1>(xv, acc);
+        // predicated groups of 4 (as the one-pass kernel): a row's remote
+        // neighbour reads are in flight together
+        for (int32_t k = 0; k < w; k += 4) {
+          int32_t c[4];
+          HVal<F, CPLX_H> h[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const bool v = k + u < w;
+            const int32_t e = off + l + (k + u) * 32;
+            c[u] = v ? cols[e] : row0 + li;                          // padding: own row
+            h[u] = v ? HVal<F, CPLX_H>::load_smem(vals, e) : HVal<F, CPLX_H>::zero();
+          }
+          LaneV<F, 1> xv[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const CT* xr = cl.map_shared_rank(x, (unsigned)(c[u] >> L.lg_rpc));
+            const CT v = xr[c[u] & (L.rpc - 1)];
+            xv[u].re[0] = v.x;
+            xv[u].im[0] = v.y;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) h[u].template fma<1>(xv[u], acc);
         }
         if (first) {
           out = acc;
