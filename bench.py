@@ -643,8 +643,9 @@ def run_small(args):
     t = 1, H~ = H / 4.05, M = 256, R = 8 random-phase vectors (seed 0), Jackson
     kernel, rho on 1,024 energies in [-4, 4].  Launch/latency bound (a 512 KB
     vector block): reports per-solve latency p50/p99 over --steps solves of the
-    resident plan (FP64, mixed and double-float, doubling; the one-launch
-    recursion against per-step launches with and without graph replay), the
+    resident plan (FP64, mixed and double-float, doubling; per-step launches
+    replayed as a CUDA graph, without the graph, and the opt-in one-launch
+    cluster recursion), the
     drop-in C-ABI call with host buffers (H~ uploaded every call, as the
     reference's cuSPARSE path does), and the CPU oracle on the whole solve."""
     import torch
@@ -668,9 +669,9 @@ def run_small(args):
     out = {"small_dos": "square 64x64 PBC, t=1, a=4.05, M=256, R=8, Jackson, 1024 energies", "sites": N,
            "solves": steps}
     ref_mu = None
-    for name, prec, extra in (("fp64", "fp64", 0), ("fp64_per_step_graph", "fp64", capi.FLAG_NO_PERSISTENT),
-                              ("fp64_per_step_launches", "fp64", capi.FLAG_NO_PERSISTENT | capi.FLAG_NO_GRAPH),
-                              ("mixed", "mixed", 0), ("dd", "dd", 0)):
+    for name, prec, extra in (("fp64", "fp64", 0), ("fp64_no_graph", "fp64", capi.FLAG_NO_GRAPH),
+                              ("fp64_cluster", "fp64", capi.FLAG_PERSISTENT), ("mixed", "mixed", 0),
+                              ("mixed_cluster", "mixed", capi.FLAG_PERSISTENT), ("dd", "dd", 0)):
         sol = tb.KpmSolver(Ht, R, precision=prec, doubling=True, flags=capi.FLAG_DEVICE_PTRS | extra)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * steps)]
         for _ in range(args.warmup + 2):

@@ -66,11 +66,12 @@ enum {
   TBK_FLAG_NO_GRAPH = 1 << 9,     /* never replay the recursion as a CUDA graph
                                      (small single-chunk plans capture their
                                      launch sequence on the second identical run) */
-  TBK_FLAG_NO_PERSISTENT = 1 << 10 /* one launch per recursion step even when the
-                                     two work vectors of a random vector fit in
-                                     shared memory (by default such plans run the
-                                     whole recursion in one launch, one CTA per
-                                     random vector)                             */
+  TBK_FLAG_PERSISTENT = 1 << 10   /* small single-chunk plans: the whole recursion
+                                     in one launch, one thread-block cluster per
+                                     random vector holding its rows and H~ in
+                                     shared memory (opt-in: on the 4,096-site
+                                     case it matches graph replay in complex64
+                                     and is slower in FP64)                     */
 };
 
 /* =========================================================================

@@ -140,12 +140,12 @@ def test_resident_plan_is_deterministic_and_random_kets(gpu):
     f = tb.KpmSolver(G.scaled_HE, 16, precision="fp64", doubling=True)
     assert _err(f.run_random(128, 5), ref) <= 1e-10
     ms, launches, bytes_ = s.last_timing()
-    assert launches == 1 and ms > 0 and bytes_ > 0        # 2,048 sites: one-launch recursion
+    assert launches == 65 and ms > 0 and bytes_ > 0
     from tight_binding_gb300 import capi
-    m = tb.KpmSolver(G.scaled_HE, 16, precision="mixed", doubling=True, flags=capi.FLAG_NO_PERSISTENT)
+    m = tb.KpmSolver(G.scaled_HE, 16, precision="mixed", doubling=True, flags=capi.FLAG_PERSISTENT)
     assert _err(m.run_random(128, 5), ref) <= MIXED_TOL
     ms, launches, bytes_ = m.last_timing()
-    assert launches == 65 and ms > 0 and bytes_ > 0
+    assert launches == 1 and ms > 0 and bytes_ > 0        # 2,048 sites: one-launch recursion
 
 
 def test_errors(gpu):
@@ -237,9 +237,8 @@ def test_graph_replay_matches_direct_launches(gpu, precision, doubling):
     G, cp, ri, v = _rescaled_csc(tb, H, 4.6)
     kets = tb.bases_of_uniform_ampl_with_random_phases(64 * 64, 8, 0)
     bras = kets if doubling else tb.bases_of_uniform_ampl_with_random_phases(64 * 64, 8, 1)
-    multi = capi.FLAG_NO_PERSISTENT
-    g = tb.KpmSolver(G.scaled_HE, 8, precision=precision, doubling=doubling, flags=multi)
-    d = tb.KpmSolver(G.scaled_HE, 8, precision=precision, doubling=doubling, flags=multi | capi.FLAG_NO_GRAPH)
+    g = tb.KpmSolver(G.scaled_HE, 8, precision=precision, doubling=doubling)
+    d = tb.KpmSolver(G.scaled_HE, 8, precision=precision, doubling=doubling, flags=capi.FLAG_NO_GRAPH)
     for M in (256, 256, 256, 256, 100, 100, 100, 256):
         a = g.run(M, bras, kets)
         b = d.run(M, bras, kets)
@@ -253,9 +252,9 @@ def test_graph_replay_matches_direct_launches(gpu, precision, doubling):
                                                        ("mixed", True, True, 8), ("mixed", False, False, 5),
                                                        ("dd", True, False, 4), ("dd", False, True, 2)])
 def test_one_launch_recursion_matches_oracle(gpu, precision, doubling, cplx, R):
-    """Plans whose two work vectors per random vector fit in shared memory run
-    the whole recursion in one launch (one CTA per vector): moments against the
-    oracle and against the one-launch-per-step path."""
+    """TBK_FLAG_PERSISTENT: the whole recursion in one launch, one thread-block
+    cluster per random vector: moments against the oracle and against the
+    one-launch-per-step path."""
     tb = gpu
     from tight_binding_gb300 import capi
 
@@ -265,8 +264,8 @@ def test_one_launch_recursion_matches_oracle(gpu, precision, doubling, cplx, R):
     n = H.shape[0]
     kets = tb.bases_of_uniform_ampl_with_random_phases(n, R, 2)
     bras = kets if doubling else tb.bases_of_uniform_ampl_with_random_phases(n, R, 3)
-    one = tb.KpmSolver(G.scaled_HE, R, precision=precision, doubling=doubling)
-    multi = tb.KpmSolver(G.scaled_HE, R, precision=precision, doubling=doubling, flags=capi.FLAG_NO_PERSISTENT)
+    one = tb.KpmSolver(G.scaled_HE, R, precision=precision, doubling=doubling, flags=capi.FLAG_PERSISTENT)
+    multi = tb.KpmSolver(G.scaled_HE, R, precision=precision, doubling=doubling)
     M = 300
     a = one.run(M, bras, kets)
     assert one.last_timing()[1] == 1                     # one recursion launch

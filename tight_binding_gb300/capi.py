@@ -32,7 +32,7 @@ FLAG_NO_L2_ZIGZAG = 1 << 6
 FLAG_STAGED = 1 << 7
 FLAG_TWO_STEP = 1 << 8
 FLAG_NO_GRAPH = 1 << 9
-FLAG_NO_PERSISTENT = 1 << 10
+FLAG_PERSISTENT = 1 << 10
 
 BUILD_SPARSE = 0
 BUILD_PERIODIC_BARE = 1

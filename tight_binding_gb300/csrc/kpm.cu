@@ -654,7 +654,7 @@ static void* small_kernel(int prec, bool cplx, bool braket) {
 static int plan_small(tbk_kpm_s* P, bool tma) {
   if (P->small_state != 0) return TBK_OK;
   P->small_state = -1;
-  if (P->n_chunks != 1 || tma || (P->flags & (TBK_FLAG_NO_PERSISTENT | TBK_FLAG_TWO_STEP))) return TBK_OK;
+  if (!(P->flags & TBK_FLAG_PERSISTENT) || P->n_chunks != 1 || tma || (P->flags & TBK_FLAG_TWO_STEP)) return TBK_OK;
   const EllDev& E = P->H->ell;
   const int32_t n = (int32_t)P->n;
   int32_t rpc = 32, lg = 5;

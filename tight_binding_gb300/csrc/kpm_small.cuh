@@ -16,6 +16,13 @@
 //
 // Partials: part[(step * 2 + slot) * nblk + CTA], the layout the fixed-order
 // reduction of the multi-launch path reads (one chunk).
+//
+// Opt-in (TBK_FLAG_PERSISTENT).  Measured on the 4,096-site, 8-vector case
+// (M = 256): 0.84 ms FP64 and 0.57 ms complex64 per solve, against 0.71 ms and
+// 0.58 ms for the per-step kernels replayed as a CUDA graph.  The steps stall
+// on distributed-shared-memory reads and the cluster barrier (short-scoreboard
+// and barrier stalls dominate), and FP64 work on 64 SMs meets GB300's slow
+// FP64 pipe.
 #pragma once
 #include <cooperative_groups.h>
 
