@@ -14,6 +14,9 @@
 //   6. GreenFunction(N, H): the Lanczos range of a ring is [-2, 2] (1e-8) and
 //      a = 4 / (2 - 0.01)
 //   7. time_evolve on the ring: plane wave k picks up exp(-i 2 cos(k) t) (1e-11)
+//   8. remove_atoms_random on a honeycomb: the open-BC Hamiltonian keeps
+//      total - n columns with entries, the rest empty (compressed index)
+//   9. moment file round trip through tbk_moments_save / tbk_moments_load
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -178,6 +181,47 @@ int main() {
     double err = 0.0;
     for (int i = 0; i < L; ++i) err = std::fmax(err, std::abs(out(i, 0) - ph * psi(i, 0)));
     expect(err <= 1e-11, "time_evolve plane wave phase", err);
+  }
+  // ---- 8. vacancies
+  {
+    UnitCell<2> hc({{1.5, 0.8660254037844386, 0}, {1.5, -0.8660254037844386, 0}}, {{"A", {0, 0, 0}}, {"B", {1, 0, 0}}});
+    hc.add_hopping("A", 1, Complex(-2.7, 0.0));
+    PartialLattice<2> X(hc, {32, 24});
+    X.remove_atoms_random("B", 100, 7);
+    X.remove_atoms("A", {{0, 0}, {5, 6}});
+    SparseMatrix H = X.get_Hamiltonian_sparse<double>();
+    std::vector<int32_t> cp, ri;
+    std::vector<double> v;
+    H.download(cp, ri, v);
+    const int kept = 2 * 32 * 24 - 102;
+    // columns past the kept count are empty; the kept block holds the bonds
+    int nonempty = 0;
+    for (int j = 0; j < kept; ++j) nonempty += cp[j + 1] > cp[j];
+    const bool ok = cp.size() == (size_t)(2 * 32 * 24 + 1) && cp[kept] == cp.back() && nonempty > kept - 20 &&
+                    cp.back() % 2 == 0;
+    expect(ok, "remove_atoms(_random): compressed open-BC Hamiltonian", (double)nonempty);
+  }
+  // ---- 9. moment files
+  {
+    std::vector<double> mu(300);
+    for (size_t k = 0; k < mu.size(); ++k) mu[k] = std::cos(0.1 * (double)k) / (1.0 + (double)k);
+    tbk_moments_header h{};
+    h.kind = TBK_MOMENTS_DOS;
+    h.rows = (int32_t)mu.size();
+    h.cols = 1;
+    h.R = 8;
+    h.seed = 42;
+    h.e_min = -4.05;
+    h.e_max = 4.05;
+    std::snprintf(h.label, sizeof(h.label), "square 64x64");
+    const char* path = "tbk_cpp_moments.tbm";
+    check(tbk_moments_save(path, &h, mu.data()));
+    tbk_moments_header g{};
+    std::vector<double> back(mu.size());
+    check(tbk_moments_load(path, &g, back.data(), (int64_t)back.size()));
+    std::remove(path);
+    const bool ok = back == mu && g.R == 8 && g.seed == 42 && std::string(g.label) == "square 64x64";
+    expect(ok, "moment file round trip", 0.0);
   }
   std::printf("%s\n", failures ? "FAILED" : "ALL PASSED");
   return failures ? 1 : 0;
