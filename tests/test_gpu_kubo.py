@@ -195,3 +195,24 @@ def test_bastin_sigma_xy_mixed_recursion(gpu):
     eps = tb.chebyshev_nodes(N)
     E, sr, si = orc.bastin_integrate(eps, orc.bastin_zeta(mu, eps, 1.0))
     assert _rel(out["sigma_re"], sr) <= 1e-5, _rel(out["sigma_re"], sr)
+
+
+@pytest.mark.parametrize("recursion", ["dd", "fp64", "mixed"])
+@pytest.mark.parametrize("which", ["bastin", "greenwood"])
+def test_fused_operator_products_same_bits(gpu, which, recursion):
+    """The output operator (a commutator, H~'s sparsity) applied inside the
+    recursion step stores the same complex64 bits as its own pass."""
+    tb = gpu
+    X, H = _system(tb, L=(20, 16))
+    G = tb.GreenFunction(48, H, -4.1, 4.1)
+    Ht = G.scaled_HE
+    v_x = tb.commutator(Ht, X.op_position(0))
+    v_y = tb.commutator(Ht, X.op_position(1))
+    kw = dict(M=48, R=4, seed=3, kernel=tb.Lorentz(6.0), tensor=True, recursion=recursion)
+    if which == "bastin":
+        a = tb.kubo_mu(Ht, None, None, v_x, v_y, **kw)
+        b = tb.kubo_mu(Ht, None, None, v_x, v_y, fuse_ops=False, **kw)
+    else:
+        a = tb.kubo_mu(Ht, v_x, v_x, None, None, **kw)
+        b = tb.kubo_mu(Ht, v_x, v_x, None, None, fuse_ops=False, **kw)
+    assert np.array_equal(a, b)

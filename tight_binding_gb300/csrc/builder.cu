@@ -115,6 +115,39 @@ int sm_count() {
   return sms;
 }
 
+// ------------------------------------------------------------------ ELL structure comparison
+__global__ void diff_i32_kernel(int64_t n, const int32_t* __restrict__ a, const int32_t* __restrict__ b,
+                                int* __restrict__ flag) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (a[i] != b[i]) *flag = 1;
+}
+
+int same_ell_structure(tbk_sparse_s* A, tbk_sparse_s* B, bool* same, cudaStream_t st) {
+  *same = false;
+  TBK_TRY(ensure_ell(A, st));
+  TBK_TRY(ensure_ell(B, st));
+  const EllDev& a = A->ell;
+  const EllDev& b = B->ell;
+  if (a.n_rows != b.n_rows || a.n_slices != b.n_slices || a.n_entries != b.n_entries || a.cplx != b.cplx)
+    return TBK_OK;
+  DevBuf flag;
+  TBK_TRY(flag.alloc(sizeof(int)));
+  TBK_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), st));
+  const int g = 4 * sm_count();
+  diff_i32_kernel<<<g, 256, 0, st>>>((int64_t)a.n_slices + 1, a.slice_off.as<int32_t>(), b.slice_off.as<int32_t>(),
+                                     flag.as<int>());
+  TBK_CHECK_LAUNCH();
+  if (a.n_entries > 0) {
+    diff_i32_kernel<<<g, 256, 0, st>>>(a.n_entries, a.col.as<int32_t>(), b.col.as<int32_t>(), flag.as<int>());
+    TBK_CHECK_LAUNCH();
+  }
+  int h = 1;
+  TBK_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  *same = h == 0;
+  return TBK_OK;
+}
+
 // ------------------------------------------------------------------ vacancies
 __global__ void keep_flags_kernel(int64_t n, const uint8_t* __restrict__ removed, int32_t* __restrict__ keep) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)

@@ -43,16 +43,19 @@ constexpr int kStepWarps = kStepThreads / 32;
 //                            FIRST: part[1] += <x|H x> (= <v_0|v_1>)
 //   braket:                  part[0] += <b|v_{s+1}>;  FIRST also part[1] += <b|x>
 //   gather == 0: no product at all (the last doubling step only needs the dots).
-//   KST: also write the output into a complex64 K-tiled store (Kubo blocks); a
-//   template flag because even an untaken runtime branch there costs the
-//   moments recursion ~8% of its bandwidth.
-template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET, bool KST = false>
+//   KST: also write a complex64 K-tiled store (Kubo blocks): 1 = the output,
+//   2 = V x for a second operator V with the same ELL structure as H (values
+//   vval / vdiag), from the same gathered x (the operator product of the
+//   previous block, fused into the step).  A template parameter because even
+//   an untaken runtime branch there costs the moments recursion ~8% of its
+//   bandwidth.
+template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET, int KST = 0>
 __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     int32_t n, int32_t n_tiles, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
     const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
     typename C2<F>::T* y, const typename C2<F>::T* pv, const typename C2<F>::T* __restrict__ bras,
     double* __restrict__ part, int store, int reverse, int gather, int pf_dist, float2* __restrict__ kstore,
-    int32_t kM, int32_t km) {
+    int32_t kM, int32_t km, const F* __restrict__ vval, const F* __restrict__ vdiag) {
   using CT = typename C2<F>::T;
   constexpr int VPL = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
   constexpr int LPR = R / VPL;             // lanes per row
@@ -91,11 +94,16 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     const LaneV<F, VPL> xs = ld_ro<F, VPL>(x + me * VPL);
     LaneV<F, VPL> prev;
     if constexpr (!FIRST) prev = ld_stream<F, VPL>(pv + me * VPL);   // pv == y: in place
-    LaneV<F, VPL> acc;
+    LaneV<F, VPL> acc, vacc;
 #pragma unroll
     for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
+    if constexpr (KST == 2) {
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) { vacc.re[q] = 0; vacc.im[q] = 0; }
+    }
     if (gather) {
       HVal<F, CPLX_H>::load(diag, r).template fma<VPL>(xs, acc);
+      if constexpr (KST == 2) HVal<F, CPLX_H>::load(vdiag, r).template fma<VPL>(xs, vacc);
       const int32_t s = r >> 5, l = r & 31;
       const int32_t off = soff[s];
       const int32_t w = (soff[s + 1] - off) >> 5;
@@ -115,6 +123,14 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
         for (int u = 0; u < 4; ++u) xv[u] = ld_ro<F, VPL>(x + ((int64_t)c[u] * LPR + sub) * VPL);
 #pragma unroll
         for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
+        if constexpr (KST == 2) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const HVal<F, CPLX_H> hv = k + u < w ? HVal<F, CPLX_H>::load(vval, off + l + (int64_t)(k + u) * 32)
+                                                 : HVal<F, CPLX_H>::zero();
+            hv.template fma<VPL>(xv[u], vacc);
+          }
+        }
       }
     }
     LaneV<F, VPL> out;
@@ -140,13 +156,14 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
       }
     }
     if (store) st_v<F, VPL>(y + me * VPL, out);
-    if constexpr (KST) {
+    if constexpr (KST != 0) {
       // block km of a complex64 K-tiled store (element k of block m at
       // ((k/16)*kM + m)*16 + k%16, k = row * R + vector): one rounding per value
+      const LaneV<F, VPL>& sv = KST == 2 ? vacc : out;
 #pragma unroll
       for (int q = 0; q < VPL; ++q) {
         const int64_t k = (int64_t)r * R + sub * VPL + q;
-        kstore[((k >> 4) * kM + km) * 16 + (k & 15)] = make_float2(to_f32(out.re[q]), to_f32(out.im[q]));
+        kstore[((k >> 4) * kM + km) * 16 + (k & 15)] = make_float2(to_f32(sv.re[q]), to_f32(sv.im[q]));
       }
     }
   }
@@ -279,6 +296,8 @@ struct StepArgs {
   int store, reverse, gather, pf_dist;
   float2* kstore = nullptr;   // optional complex64 K-tiled copy of the output (Kubo blocks)
   int32_t kM = 0, km = 0;
+  const void* vval = nullptr;  // with kstore: store V x instead (V shares the ELL structure)
+  const void* vdiag = nullptr;
 };
 
 template <typename F, int R, bool CPLX_H>
@@ -290,15 +309,18 @@ static int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
   auto b = static_cast<const CT*>(a.bras);
   auto ev = static_cast<const F*>(a.eval);
   auto dg = static_cast<const F*>(a.diag);
+  auto vv = static_cast<const F*>(a.vval);
+  auto vd = static_cast<const F*>(a.vdiag);
 #define TBK_STEP(FI, BR, KS)                                                               \
   kpm_step_kernel<F, R, CPLX_H, FI, BR, KS><<<grid, kStepThreads, 0, st>>>(                \
       a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.kstore, \
-      a.kM, a.km)
+      a.kM, a.km, vv, vd)
   if (a.kstore) {
     if (braket) return fail(TBK_ERR_UNSUPPORTED, "K-tiled store with a braket step");
-    if (first) TBK_STEP(true, false, true); else TBK_STEP(false, false, true);
-  } else if (first) { if (braket) TBK_STEP(true, true, false); else TBK_STEP(true, false, false); }
-  else { if (braket) TBK_STEP(false, true, false); else TBK_STEP(false, false, false); }
+    if (a.vval) { if (first) TBK_STEP(true, false, 2); else TBK_STEP(false, false, 2); }
+    else { if (first) TBK_STEP(true, false, 1); else TBK_STEP(false, false, 1); }
+  } else if (first) { if (braket) TBK_STEP(true, true, 0); else TBK_STEP(true, false, 0); }
+  else { if (braket) TBK_STEP(false, true, 0); else TBK_STEP(false, false, 0); }
 #undef TBK_STEP
   TBK_CHECK_LAUNCH();
   return TBK_OK;
@@ -427,7 +449,8 @@ int step_config(tbk_sparse_s* A, int Rc, int prec, int* grid, int* n_tiles, cuda
 }
 
 int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
-             int grid, int n_tiles, cudaStream_t st, float2* kstore, int32_t kM, int32_t km, bool store_y) {
+             int grid, int n_tiles, cudaStream_t st, float2* kstore, int32_t kM, int32_t km, bool store_y,
+             tbk_sparse_s* vop) {
   StepArgs a;
   a.n = A->rows;
   a.n_tiles = n_tiles;
@@ -449,6 +472,11 @@ int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const vo
   a.kstore = kstore;
   a.kM = kM;
   a.km = km;
+  if (vop) {
+    if (!kstore) return fail(TBK_ERR_INVALID, "operator product without a store");
+    a.vval = ell_vals(vop->ell, prec);
+    a.vdiag = ell_diag(vop->ell, prec);
+  }
   const bool c = A->ell.cplx != 0;
   if (prec == TBK_PREC_FP64)
     return c ? launch_step<double, true>(Rc, a, first, false, grid, st) : launch_step<double, false>(Rc, a, first, false, grid, st);

@@ -130,9 +130,13 @@ int sm_count();
 int step_config(tbk_sparse_s* A, int Rc, int prec, int* grid, int* n_tiles, cudaStream_t st);
 // kstore: optional complex64 K-tiled store that receives the step's output as
 // block km of kM (store_y false: only there)
+// vop: with kstore, store vop x instead of the output; vop must share A's ELL
+// structure (same_ell_structure) and precision arrays
 int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
              int grid, int n_tiles, cudaStream_t st, float2* kstore = nullptr, int32_t kM = 0, int32_t km = 0,
-             bool store_y = true);
+             bool store_y = true, tbk_sparse_s* vop = nullptr);
+// true when B's sliced ELL has A's slices, widths and columns (values may differ)
+int same_ell_structure(tbk_sparse_s* A, tbk_sparse_s* B, bool* same, cudaStream_t st);
 int load_block_any(int prec, int32_t n, int32_t R, int32_t r0, int32_t Rp, const double2* src, void* dst,
                    cudaStream_t st);
 int random_block_any(int prec, int32_t n, int32_t R, int32_t r0, int32_t Rp, uint64_t seed, void* dst,
