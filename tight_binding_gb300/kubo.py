@@ -101,7 +101,7 @@ def bastin_integrate(eps, zeta):
 
 def conductivity_Kubo_Bastin(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMatrix, N: int, E_min: float,
                              E_max: float, Volume: float = 1.0, R: int = 4, seed: int = 0, kernel: Kernel | None = None,
-                             tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd"):
+                             tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd", fuse_ops: bool = True):
     """TB/snippets.h:306-456: G(N, H, E_min-1e-8, E_max+1e-8); v = X H~ - H~ X;
     aL = g T r, aR = g v_x T v_y r; zeta at the N Chebyshev nodes; cumulative
     integral from E = 0.  Returns dict with eps, zeta, E, sigma_re, sigma_im, mu."""
@@ -111,7 +111,7 @@ def conductivity_Kubo_Bastin(H_og: SparseMatrix, op_x: SparseMatrix, op_y: Spars
     v_x = commutator(Ht, op_x)
     v_y = commutator(Ht, op_y)
     mu = kubo_mu(Ht, None, None, v_x, v_y, N, R, seed, kernel=kernel, tensor=tensor, budget_gb=budget_gb,
-                 recursion=recursion)
+                 recursion=recursion, fuse_ops=fuse_ops)
     eps = chebyshev_nodes(N)
     zeta = bastin_zeta(mu, eps, Volume)
     E, sr, si = bastin_integrate(eps, zeta)
@@ -120,7 +120,7 @@ def conductivity_Kubo_Bastin(H_og: SparseMatrix, op_x: SparseMatrix, op_y: Spars
 
 def conductivity_spectrum(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMatrix, N: int, R: int = 128,
                           seed: int = 0, kernel: Kernel | None = None, E_min: float = -4.0001, E_max: float = 4.0001,
-                          tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd"):
+                          tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd", fuse_ops: bool = True):
     """Kubo-Greenwood spectrum, TB/snippets.h:225-304: aR = g T r, aL = g v_x T v_x r,
     sigma(eps_k) = -<phi_L|phi_R> w(eps_k)^2 / R at the N Chebyshev nodes."""
     kernel = kernel if kernel is not None else Lorentz(6.0)
@@ -128,7 +128,7 @@ def conductivity_spectrum(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMa
     Ht = G.scaled_HE
     v_x = commutator(Ht, op_x)
     mu = kubo_mu(Ht, v_x, v_x, None, None, N, R, seed, kernel=kernel, tensor=tensor, budget_gb=budget_gb,
-                 recursion=recursion)
+                 recursion=recursion, fuse_ops=fuse_ops)
     eps = chebyshev_nodes(N)
     return eps, greenwood_sigma(mu, eps, R), mu
 
