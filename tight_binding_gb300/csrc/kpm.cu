@@ -133,6 +133,8 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
         }
       }
     }
+    finish_acc<F, VPL>(acc);
+    if constexpr (KST == 2) finish_acc<F, VPL>(vacc);
     LaneV<F, VPL> out;
 #pragma unroll
     for (int q = 0; q < VPL; ++q) {

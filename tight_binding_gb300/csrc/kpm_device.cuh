@@ -46,6 +46,28 @@ __device__ __forceinline__ dd operator*(dd a, dd b) {
   return dd_fast_two_sum(p, e);
 }
 __device__ __forceinline__ dd& operator+=(dd& a, dd b) { a = a + b; return a; }
+// acc += h x for a row sum, accumulated unnormalised in the manner of Dot2
+// (Ogita, Rump & Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput.
+// 26(6), 2005): the product's leading term and its exact FMA error, the two
+// cross terms, and the exact TwoSum error of the running sum all go into acc.lo
+// with plain adds; acc.hi carries the running FP32 sum.  The dependency chain
+// between entries is one add; dd_norm restores a normalised pair afterwards.
+__device__ __forceinline__ void dd_fma_acc(dd h, dd x, dd& acc) {
+  const float p = __fmul_rn(h.hi, x.hi);
+  float e = __fmaf_rn(h.hi, x.hi, -p);
+  e = __fmaf_rn(h.hi, x.lo, e);
+  e = __fmaf_rn(h.lo, x.hi, e);
+  const float s = __fadd_rn(acc.hi, p);
+  const float bb = __fsub_rn(s, acc.hi);
+  const float t = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  acc.hi = s;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(t, e));
+}
+__device__ __forceinline__ dd dd_norm(dd a) {            // TwoSum(hi, lo)
+  const float s = __fadd_rn(a.hi, a.lo);
+  const float bb = __fsub_rn(s, a.hi);
+  return dd(s, __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(a.lo, bb)));
+}
 struct __align__(16) dd2 {
   dd x, y;
 };
@@ -141,7 +163,15 @@ struct HVal<F, false> {
   template <int VPL>
   __device__ __forceinline__ void fma(const LaneV<F, VPL>& x, LaneV<F, VPL>& acc) const {
 #pragma unroll
-    for (int q = 0; q < VPL; ++q) { acc.re[q] = fma_(v, x.re[q], acc.re[q]); acc.im[q] = fma_(v, x.im[q], acc.im[q]); }
+    for (int q = 0; q < VPL; ++q) {
+      if constexpr (is_dd<F>) {
+        dd_fma_acc(v, x.re[q], acc.re[q]);
+        dd_fma_acc(v, x.im[q], acc.im[q]);
+      } else {
+        acc.re[q] = fma_(v, x.re[q], acc.re[q]);
+        acc.im[q] = fma_(v, x.im[q], acc.im[q]);
+      }
+    }
   }
   __device__ __forceinline__ static F fma_(F a, F b, F c) { return a * b + c; }
 };
@@ -166,13 +196,33 @@ struct HVal<F, true> {
   __device__ __forceinline__ void fma(const LaneV<F, VPL>& x, LaneV<F, VPL>& acc) const {
 #pragma unroll
     for (int q = 0; q < VPL; ++q) {
-      acc.re[q] = r * x.re[q] + acc.re[q];
-      acc.re[q] = -i * x.im[q] + acc.re[q];
-      acc.im[q] = r * x.im[q] + acc.im[q];
-      acc.im[q] = i * x.re[q] + acc.im[q];
+      if constexpr (is_dd<F>) {
+        dd_fma_acc(r, x.re[q], acc.re[q]);
+        dd_fma_acc(-i, x.im[q], acc.re[q]);
+        dd_fma_acc(r, x.im[q], acc.im[q]);
+        dd_fma_acc(i, x.re[q], acc.im[q]);
+      } else {
+        acc.re[q] = r * x.re[q] + acc.re[q];
+        acc.re[q] = -i * x.im[q] + acc.re[q];
+        acc.im[q] = r * x.im[q] + acc.im[q];
+        acc.im[q] = i * x.re[q] + acc.im[q];
+      }
     }
   }
 };
+
+// a row sum built by HVal::fma, ready for use: double-float sums are
+// normalised (no-op for float and double)
+template <typename F, int VPL>
+__device__ __forceinline__ void finish_acc(LaneV<F, VPL>& acc) {
+  if constexpr (is_dd<F>) {
+#pragma unroll
+    for (int q = 0; q < VPL; ++q) {
+      acc.re[q] = dd_norm(acc.re[q]);
+      acc.im[q] = dd_norm(acc.im[q]);
+    }
+  }
+}
 
 template <typename F> struct VecW { static constexpr int max_vpl = (sizeof(F) == 4) ? 2 : 1; };
 template <> struct VecW<dd> { static constexpr int max_vpl = 1; };

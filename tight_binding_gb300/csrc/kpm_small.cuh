@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(kSmallThreadsMax) kpm_cluster_kernel(
 #pragma unroll
           for (int u = 0; u < 4; ++u) h[u].template fma<1>(xv[u], acc);
         }
+        finish_acc<F, 1>(acc);
         if (first) {
           out = acc;
         } else {

@@ -184,6 +184,7 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
           for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
         }
       }
+      finish_acc<F, VPL>(acc);
       LaneV<F, VPL> out;
 #pragma unroll
       for (int q = 0; q < VPL; ++q) {
