@@ -401,7 +401,8 @@ def peaks_tensor():
     return 1900.0 / 2.0, "half of fallback bf16"
 
 
-def run_kubo(config: int, tensor: bool = True, recursion: str = "dd", fuse_ops: bool = True):
+def run_kubo(config: int, tensor: bool = True, recursion: str = "dd", fuse_ops: bool = True, moments: int = 0,
+             budget_gb: float = 0.0):
     """Kubo legs: config 3 (Bastin sigma_xy, square 256^2 open-x / periodic-y, Landau
     flux 1/64, M = 512, R = 16, seed 2) or config 5 (Greenwood sigma_xx, FCC 128^3
     periodic, on-site U[-1,1] seed 4, M = 1024, R = 8)."""
@@ -409,24 +410,24 @@ def run_kubo(config: int, tensor: bool = True, recursion: str = "dd", fuse_ops: 
 
     t0 = time.perf_counter()
     if config == 3:
-        L, M, R = 256, 512, 16
+        L, M, R = 256, moments or 512, 16
         X = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (L, L))
         G = np.zeros((3, 3))
         G[1, 0] = 2 * np.pi / 64
         X.set_gauge_linear(G, np.zeros(3))
         H = X.get_Hamiltonian_periodic_extend_bare_sparse([0, 1], complex)
         out = tb.conductivity_Kubo_Bastin(H, X.op_position(0), X.op_position(1), M, -4.0, 4.0, R=R, seed=2,
-                                          tensor=tensor, recursion=recursion, fuse_ops=fuse_ops)
+                                          tensor=tensor, recursion=recursion, fuse_ops=fuse_ops, budget_gb=budget_gb)
         result = {"E_F_points": int(len(out["E"])), "sigma_xy_at_E0": float(out["sigma_re"][len(out["E"]) // 2])}
         workload = "Kubo-Bastin sigma_xy: square 256x256 open-x/periodic-y, Landau flux 1/64, M=512, R=16 seed 2"
     else:
-        L, M, R = 128, 1024, 8
+        L, M, R = 128, moments or 1024, 8
         X = tb.PartialLattice(tb.FCC().add_hopping("A", 1, 1.0), (L, L, L))
         X.set_scalar_disorder(2.0, 4)
         H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1, 1], complex)
         eps, sigma, mu = tb.conductivity_spectrum(H, X.op_position(0), X.op_position(1), M, R=R, seed=4,
                                                   E_min=-13.0, E_max=13.0, tensor=tensor, recursion=recursion,
-                                                  fuse_ops=fuse_ops)
+                                                  fuse_ops=fuse_ops, budget_gb=budget_gb)
         result = {"energies": int(len(eps)), "sigma_xx_max": float(np.max(sigma))}
         workload = "Kubo-Greenwood sigma_xx: FCC 128^3 periodic, disorder U[-1,1] seed 4, M=1024, R=8"
     wall = time.perf_counter() - t0
@@ -434,7 +435,7 @@ def run_kubo(config: int, tensor: bool = True, recursion: str = "dd", fuse_ops: 
     peak, src = peaks_tensor()
     useful = tmg["gemm_flops"] / (3.0 if tensor else 1.0)       # one complex GEMM = 8 M^2 K real flops
     line = {"workload": workload, "path": "tcgen05 3xTF32" if tensor else "CUDA-core FP32", "recursion": recursion,
-            "fused_operator_products": fuse_ops,
+            "fused_operator_products": fuse_ops, "moments": M,
             "wall_s": wall, "blocks_ms": tmg["ms_blocks"], "gemm_ms": tmg["ms_gemm"], "chunks": tmg["chunks"],
             "gemm_tflops_issued": tmg["gemm_flops"] / (tmg["ms_gemm"] / 1e3) / 1e12,
             "gemm_tflops_useful": useful / (tmg["ms_gemm"] / 1e3) / 1e12,
@@ -769,6 +770,10 @@ def main():
     ap.add_argument("--cuda-core-mu", action="store_true", help="Kubo leg with the CUDA-core mu GEMM")
     ap.add_argument("--kubo-recursion", default="dd", choices=["fp64", "mixed", "dd"],
                     help="stored-block recursion: double-float (default), complex128 or complex64")
+    ap.add_argument("--kubo-moments", type=int, default=0,
+                    help="override M of the Kubo leg (small profiling case; not the benchmark)")
+    ap.add_argument("--kubo-budget-gb", type=float, default=0.0,
+                    help="stored-block budget of the Kubo leg (0: 60%% of free memory)")
     ap.add_argument("--kubo-unfused", action="store_true",
                     help="Kubo leg with the output-operator products in passes of their own (A/B)")
     ap.add_argument("--no-hopping", action="store_true",
@@ -802,7 +807,8 @@ def main():
         return run_kernel_only(args)
     if args.kubo:
         print(json.dumps(run_kubo(args.kubo, tensor=not args.cuda_core_mu, recursion=args.kubo_recursion,
-                                  fuse_ops=not args.kubo_unfused)), flush=True)
+                                  fuse_ops=not args.kubo_unfused, moments=args.kubo_moments,
+                                  budget_gb=args.kubo_budget_gb)), flush=True)
         return 0
     if args.impl == "reference":
         return run_reference(args)
