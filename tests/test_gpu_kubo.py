@@ -201,7 +201,8 @@ def test_bastin_sigma_xy_mixed_recursion(gpu):
 @pytest.mark.parametrize("which", ["bastin", "greenwood"])
 def test_fused_operator_products_same_bits(gpu, which, recursion):
     """The output operator (a commutator, H~'s sparsity) applied inside the
-    recursion step stores the same complex64 bits as its own pass."""
+    recursion step, and both sides run as one recursion of twice the width,
+    store the same complex64 bits as separate passes."""
     tb = gpu
     X, H = _system(tb, L=(20, 16))
     G = tb.GreenFunction(48, H, -4.1, 4.1)
@@ -212,7 +213,10 @@ def test_fused_operator_products_same_bits(gpu, which, recursion):
     if which == "bastin":
         a = tb.kubo_mu(Ht, None, None, v_x, v_y, **kw)
         b = tb.kubo_mu(Ht, None, None, v_x, v_y, fuse_ops=False, **kw)
+        c = tb.kubo_mu(Ht, None, None, v_x, v_y, separate_sides=True, **kw)
     else:
         a = tb.kubo_mu(Ht, v_x, v_x, None, None, **kw)
         b = tb.kubo_mu(Ht, v_x, v_x, None, None, fuse_ops=False, **kw)
-    assert np.array_equal(a, b)
+        c = tb.kubo_mu(Ht, v_x, v_x, None, None, separate_sides=True, **kw)
+    assert np.array_equal(a, b)      # both sides as one recursion vs separate passes
+    assert np.array_equal(a, c)      # vs separate sides with fused products

@@ -43,19 +43,19 @@ constexpr int kStepWarps = kStepThreads / 32;
 //                            FIRST: part[1] += <x|H x> (= <v_0|v_1>)
 //   braket:                  part[0] += <b|v_{s+1}>;  FIRST also part[1] += <b|x>
 //   gather == 0: no product at all (the last doubling step only needs the dots).
-//   KST: also write a complex64 K-tiled store (Kubo blocks): 1 = the output,
-//   2 = V x for a second operator V with the same ELL structure as H (values
-//   vval / vdiag), from the same gathered x (the operator product of the
-//   previous block, fused into the step).  A template parameter because even
-//   an untaken runtime branch there costs the moments recursion ~8% of its
-//   bandwidth.
+//   KST: also write complex64 K-tiled stores (Kubo blocks, KStore): 1 = the
+//   output into one store; 2 = per column group the output or V x for an
+//   operator V with H's ELL structure, formed from the same gathered x (the
+//   operator product of the previous block fused into the step), so that the
+//   two sides of a Kubo pair can run as one recursion of twice the width.  A
+//   template parameter because even an untaken runtime branch there costs the
+//   moments recursion ~8% of its bandwidth.
 template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET, int KST = 0>
 __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     int32_t n, int32_t n_tiles, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
     const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
     typename C2<F>::T* y, const typename C2<F>::T* pv, const typename C2<F>::T* __restrict__ bras,
-    double* __restrict__ part, int store, int reverse, int gather, int pf_dist, float2* __restrict__ kstore,
-    int32_t kM, int32_t km, const F* __restrict__ vval, const F* __restrict__ vdiag) {
+    double* __restrict__ part, int store, int reverse, int gather, int pf_dist, const KStore ks) {
   using CT = typename C2<F>::T;
   constexpr int VPL = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
   constexpr int LPR = R / VPL;             // lanes per row
@@ -97,7 +97,15 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     LaneV<F, VPL> acc, vacc;
 #pragma unroll
     for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
+    // column group of this lane (its VPL columns never straddle two groups)
+    const int grp = (KST == 2 && ks.halves == 2 && sub * VPL >= R / 2) ? 1 : 0;
+    const F* vval = nullptr;
+    const F* vdiag = nullptr;
     if constexpr (KST == 2) {
+      const void* vv = grp ? ks.vval[1] : ks.vval[0];      // selects, not an indexed parameter array
+      const void* vd = grp ? ks.vdiag[1] : ks.vdiag[0];
+      vval = vv ? static_cast<const F*>(vv) : eval;
+      vdiag = vd ? static_cast<const F*>(vd) : diag;
 #pragma unroll
       for (int q = 0; q < VPL; ++q) { vacc.re[q] = 0; vacc.im[q] = 0; }
     }
@@ -158,14 +166,24 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
       }
     }
     if (store) st_v<F, VPL>(y + me * VPL, out);
-    if constexpr (KST != 0) {
-      // block km of a complex64 K-tiled store (element k of block m at
-      // ((k/16)*kM + m)*16 + k%16, k = row * R + vector): one rounding per value
-      const LaneV<F, VPL>& sv = KST == 2 ? vacc : out;
+    if constexpr (KST == 1) {
+      // block km[0] of the K-tiled store: one rounding per value
 #pragma unroll
       for (int q = 0; q < VPL; ++q) {
         const int64_t k = (int64_t)r * R + sub * VPL + q;
-        kstore[((k >> 4) * kM + km) * 16 + (k & 15)] = make_float2(to_f32(sv.re[q]), to_f32(sv.im[q]));
+        ks.store[0][((k >> 4) * ks.kM + ks.km[0]) * 16 + (k & 15)] = make_float2(to_f32(out.re[q]), to_f32(out.im[q]));
+      }
+    } else if constexpr (KST == 2) {
+      const int32_t kmg = grp ? ks.km[1] : ks.km[0];
+      if (kmg >= 0) {
+        const int32_t Rg = R / ks.halves;
+        const LaneV<F, VPL>& sv = (grp ? ks.usev[1] : ks.usev[0]) ? vacc : out;
+        float2* dst = grp ? ks.store[1] : ks.store[0];
+#pragma unroll
+        for (int q = 0; q < VPL; ++q) {
+          const int64_t k = (int64_t)r * Rg + sub * VPL + q - grp * Rg;
+          dst[((k >> 4) * ks.kM + kmg) * 16 + (k & 15)] = make_float2(to_f32(sv.re[q]), to_f32(sv.im[q]));
+        }
       }
     }
   }
@@ -296,10 +314,8 @@ struct StepArgs {
   const void* bras;
   double* part;
   int store, reverse, gather, pf_dist;
-  float2* kstore = nullptr;   // optional complex64 K-tiled copy of the output (Kubo blocks)
-  int32_t kM = 0, km = 0;
-  const void* vval = nullptr;  // with kstore: store V x instead (V shares the ELL structure)
-  const void* vdiag = nullptr;
+  KStore ks;                   // optional complex64 K-tiled stores (Kubo blocks)
+  int kst = 0;                 // 0 none, 1 output into ks.store[0], 2 per-group output / V x
 };
 
 template <typename F, int R, bool CPLX_H>
@@ -311,15 +327,15 @@ static int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
   auto b = static_cast<const CT*>(a.bras);
   auto ev = static_cast<const F*>(a.eval);
   auto dg = static_cast<const F*>(a.diag);
-  auto vv = static_cast<const F*>(a.vval);
-  auto vd = static_cast<const F*>(a.vdiag);
 #define TBK_STEP(FI, BR, KS)                                                               \
   kpm_step_kernel<F, R, CPLX_H, FI, BR, KS><<<grid, kStepThreads, 0, st>>>(                \
-      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.kstore, \
-      a.kM, a.km, vv, vd)
-  if (a.kstore) {
+      a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.ks)
+  if (a.kst != 0) {
     if (braket) return fail(TBK_ERR_UNSUPPORTED, "K-tiled store with a braket step");
-    if (a.vval) { if (first) TBK_STEP(true, false, 2); else TBK_STEP(false, false, 2); }
+    constexpr int VPLR = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
+    if (a.kst == 2 && a.ks.halves == 2 && (R / 2) % VPLR != 0)
+      return fail(TBK_ERR_UNSUPPORTED, "column groups narrower than a lane's vectors");
+    if (a.kst == 2) { if (first) TBK_STEP(true, false, 2); else TBK_STEP(false, false, 2); }
     else { if (first) TBK_STEP(true, false, 1); else TBK_STEP(false, false, 1); }
   } else if (first) { if (braket) TBK_STEP(true, true, 0); else TBK_STEP(true, false, 0); }
   else { if (braket) TBK_STEP(false, true, 0); else TBK_STEP(false, false, 0); }
@@ -421,10 +437,10 @@ static int rows_per_tile(int prec, int Rc) {
 // ---------------------------------------------------------------- internal API
 // (used by the Kubo block recursions in kubo.cu and the server)
 // ELL value arrays of a precision: FP32, FP64 or double-float pairs.
-static const void* ell_vals(const EllDev& E, int prec) {
+const void* ell_vals(const EllDev& E, int prec) {
   return prec == TBK_PREC_MIXED ? E.val32.p : prec == TBK_PREC_DD ? E.valdd.p : E.val64.p;
 }
-static const void* ell_diag(const EllDev& E, int prec) {
+const void* ell_diag(const EllDev& E, int prec) {
   return prec == TBK_PREC_MIXED ? E.diag32.p : prec == TBK_PREC_DD ? E.diagdd.p : E.diag64.p;
 }
 
@@ -450,6 +466,8 @@ int step_config(tbk_sparse_s* A, int Rc, int prec, int* grid, int* n_tiles, cuda
   return TBK_OK;
 }
 
+static int step_dispatch(tbk_sparse_s* A, int Rc, int prec, bool first, const StepArgs& a, int grid, cudaStream_t st);
+
 int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
              int grid, int n_tiles, cudaStream_t st, float2* kstore, int32_t kM, int32_t km, bool store_y,
              tbk_sparse_s* vop) {
@@ -471,14 +489,49 @@ int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const vo
   a.reverse = 0;
   a.gather = 1;
   a.pf_dist = 1;
-  a.kstore = kstore;
-  a.kM = kM;
-  a.km = km;
-  if (vop) {
-    if (!kstore) return fail(TBK_ERR_INVALID, "operator product without a store");
-    a.vval = ell_vals(vop->ell, prec);
-    a.vdiag = ell_diag(vop->ell, prec);
+  if (kstore) {
+    a.ks.store[0] = kstore;
+    a.ks.kM = kM;
+    a.ks.km[0] = km;
+    a.kst = 1;
+    if (vop) {
+      a.ks.vval[0] = ell_vals(vop->ell, prec);
+      a.ks.vdiag[0] = ell_diag(vop->ell, prec);
+      a.ks.usev[0] = 1;
+      a.kst = 2;
+    }
+  } else if (vop) {
+    return fail(TBK_ERR_INVALID, "operator product without a store");
   }
+  return step_dispatch(A, Rc, prec, first, a, grid, st);
+}
+
+int step_ks(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
+            int grid, int n_tiles, cudaStream_t st, const KStore& ks) {
+  StepArgs a;
+  a.n = A->rows;
+  a.n_tiles = n_tiles;
+  a.n_slices = A->ell.n_slices;
+  a.err = nullptr;
+  a.soff = A->ell.slice_off.as<int32_t>();
+  a.ecol = A->ell.col.as<int32_t>();
+  a.eval = ell_vals(A->ell, prec);
+  a.diag = ell_diag(A->ell, prec);
+  a.x = x;
+  a.y = y;
+  a.pv = first ? y : pv;
+  a.bras = nullptr;
+  a.part = part;
+  a.store = 1;
+  a.reverse = 0;
+  a.gather = 1;
+  a.pf_dist = 1;
+  a.ks = ks;
+  a.kst = 2;
+  return step_dispatch(A, Rc, prec, first, a, grid, st);
+}
+
+static int step_dispatch(tbk_sparse_s* A, int Rc, int prec, bool first, const StepArgs& a, int grid, cudaStream_t st) {
   const bool c = A->ell.cplx != 0;
   if (prec == TBK_PREC_FP64)
     return c ? launch_step<double, true>(Rc, a, first, false, grid, st) : launch_step<double, false>(Rc, a, first, false, grid, st);

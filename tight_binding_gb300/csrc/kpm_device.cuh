@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "tbk_internal.h"
+
 namespace tbk {
 
 // Double-float number: value = hi + lo (|lo| <= ulp(hi) / 2), about 48

@@ -113,6 +113,28 @@ __global__ void round_block_kernel(const CT* __restrict__ src, float2* __restric
     store[((q >> 4) * M + m) * 16 + (q & 15)] = to_c64(src[q]);
 }
 
+// columns [c0, c0 + Rc) of a 2 Rc-wide site-major block <- an Rc-wide block
+template <typename CT>
+__global__ void pack_cols_kernel(int64_t n_pad, int32_t Rc, int32_t c0, const CT* __restrict__ src,
+                                 CT* __restrict__ dst) {
+  const int64_t tot = n_pad * Rc;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = q / Rc;
+    dst[row * 2 * Rc + c0 + (q - row * Rc)] = src[q];
+  }
+}
+// block m of a K-tiled store (k = row * Rc + column) <- columns [c0, c0 + Rc)
+// of a 2 Rc-wide block, rounded to complex64
+template <typename CT>
+__global__ void round_cols_kernel(int64_t n_pad, int32_t Rc, int32_t c0, const CT* __restrict__ src,
+                                  float2* __restrict__ store, int32_t m, int32_t M) {
+  const int64_t tot = n_pad * Rc;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = q / Rc;
+    store[((q >> 4) * M + m) * 16 + (q & 15)] = to_c64(src[row * 2 * Rc + c0 + (q - row * Rc)]);
+  }
+}
+
 __global__ void mu_kernel_scale_kernel(double2* __restrict__ mu, const double* __restrict__ g, int32_t M) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= (int64_t)M * M) return;
@@ -260,7 +282,18 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   const int64_t blk16 = (blk + 15) / 16 * 16;           // K padded to whole 16-element tiles (zeros)
   TBK_TRY(Ls.alloc(sizeof(float2) * blk16 * M));
   TBK_TRY(Rs.alloc(sizeof(float2) * blk16 * M));
-  TBK_TRY(work.alloc(csz * blk * 6));
+  // both sides as one recursion of width 2 Rc when every output operator can
+  // be fused into the step (the gathers move twice the bytes per row; the
+  // stored values are the same bits)
+  bool both = !(flags & (TBK_MU_SEPARATE_SIDES | TBK_MU_UNFUSED_OPS)) &&
+              2 * Rc <= (prec == TBK_PREC_MIXED ? 64 : 32) && (prec != TBK_PREC_MIXED || Rc >= 2);
+  for (tbk_sparse_s* o : {AL, AR}) {
+    if (!both || !o) continue;
+    bool same = false;
+    TBK_TRY(same_ell_structure(Ht, o, &same, st));
+    both = same;
+  }
+  TBK_TRY(work.alloc(csz * blk * (both ? 12 : 6)));
   TBK_CUDA(cudaMemsetAsync(Ls.p, 0, Ls.bytes, st));
   TBK_CUDA(cudaMemsetAsync(Rs.p, 0, Rs.bytes, st));
   TBK_CUDA(cudaMemsetAsync(work.p, 0, work.bytes, st));
@@ -275,6 +308,13 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   int gmax = grid;
   for (auto* o : ops)
     if (o) { int g2, t2; TBK_TRY(step_config(o, Rc, prec, &g2, &t2, st)); gmax = std::max(gmax, g2); }
+  int grid2 = 1, tiles2 = 1;
+  if (both) {
+    TBK_TRY(step_config(Ht, 2 * Rc, prec, &grid2, &tiles2, st));
+    gmax = std::max(gmax, grid2);
+    if (prec == TBK_PREC_DD)
+      for (tbk_sparse_s* o : {AL, AR}) if (o) TBK_TRY(ensure_ell_dd(o, st));
+  }
   TBK_TRY(partd.alloc(sizeof(double) * 2 * gmax));
   char* wb = work.as<char>();
   auto wblk = [&](int i) { return static_cast<void*>(wb + (size_t)i * blk * csz); };
@@ -332,6 +372,64 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     if (fuse) TBK_TRY(apply_to_store(Aout, r[(M - 1) % 3], tmpA, store, M - 1));
     return TBK_OK;
   };
+  // both sides at once: columns [0, Rc) carry the left side (BL v0), [Rc, 2 Rc)
+  // the right side (BR v0); step m stores T_m of a side without an output
+  // operator as block m and A T_{m-1} of a side with one as block m-1
+  auto both_sides = [&]() -> int {
+    const size_t b2 = csz * blk * 2;
+    char* base = wb + csz * blk * 6;                     // three 2 Rc-wide blocks after the six Rc-wide ones
+    void* r[3] = {base, base + b2, base + 2 * b2};
+    void* half[2] = {wblk(0), wblk(1)};
+    tbk_sparse_s* Bin[2] = {BL, BR};
+    tbk_sparse_s* Aout[2] = {AL, AR};
+    float2* stores[2] = {Ls.as<float2>(), Rs.as<float2>()};
+    const unsigned gp = (unsigned)std::min<int64_t>((blk + 255) / 256, 65535);
+    for (int h = 0; h < 2; ++h) {
+      if (Bin[h]) TBK_TRY(apply(Bin[h], v0, half[h]));
+      else TBK_CUDA(cudaMemcpyAsync(half[h], v0, csz * blk, cudaMemcpyDeviceToDevice, st));
+      if (prec == TBK_PREC_FP64)
+        pack_cols_kernel<double2><<<gp, 256, 0, st>>>(n_pad, Rc, h * Rc, static_cast<const double2*>(half[h]),
+                                                      static_cast<double2*>(r[0]));
+      else if (prec == TBK_PREC_DD)
+        pack_cols_kernel<dd2><<<gp, 256, 0, st>>>(n_pad, Rc, h * Rc, static_cast<const dd2*>(half[h]),
+                                                  static_cast<dd2*>(r[0]));
+      else
+        pack_cols_kernel<float2><<<gp, 256, 0, st>>>(n_pad, Rc, h * Rc, static_cast<const float2*>(half[h]),
+                                                     static_cast<float2*>(r[0]));
+      TBK_CHECK_LAUNCH();
+      if (!Aout[h]) {
+        if (prec == TBK_PREC_FP64)
+          round_cols_kernel<double2><<<gp, 256, 0, st>>>(n_pad, Rc, h * Rc, static_cast<const double2*>(r[0]),
+                                                         stores[h], 0, M);
+        else if (prec == TBK_PREC_DD)
+          round_cols_kernel<dd2><<<gp, 256, 0, st>>>(n_pad, Rc, h * Rc, static_cast<const dd2*>(r[0]), stores[h], 0, M);
+        else
+          round_cols_kernel<float2><<<gp, 256, 0, st>>>(n_pad, Rc, h * Rc, static_cast<const float2*>(r[0]),
+                                                        stores[h], 0, M);
+        TBK_CHECK_LAUNCH();
+      }
+    }
+    KStore ks;
+    ks.halves = 2;
+    ks.kM = M;
+    for (int h = 0; h < 2; ++h) {
+      ks.store[h] = stores[h];
+      ks.usev[h] = Aout[h] ? 1 : 0;
+      ks.vval[h] = Aout[h] ? ell_vals(Aout[h]->ell, prec) : nullptr;
+      ks.vdiag[h] = Aout[h] ? ell_diag(Aout[h]->ell, prec) : nullptr;
+    }
+    for (int32_t m = 1; m < M; ++m) {
+      for (int h = 0; h < 2; ++h) ks.km[h] = Aout[h] ? m - 1 : m;
+      TBK_TRY(step_ks(Ht, 2 * Rc, prec, r[(m - 1) % 3], r[m % 3], m >= 2 ? r[(m - 2) % 3] : nullptr, m == 1,
+                      partd.as<double>(), grid2, tiles2, st, ks));
+    }
+    if (AL || AR) {                                      // A T_{M-1} -> block M-1 (the new vector is not kept)
+      for (int h = 0; h < 2; ++h) ks.km[h] = Aout[h] ? M - 1 : -1;
+      TBK_TRY(step_ks(Ht, 2 * Rc, prec, r[(M - 1) % 3], r[M % 3], M >= 2 ? r[(M - 2) % 3] : nullptr, M == 1,
+                      partd.as<double>(), grid2, tiles2, st, ks));
+    }
+    return TBK_OK;
+  };
   const bool use_tc = (flags & TBK_MU_TENSOR) != 0;
   const int64_t ksplit = 16384;
   const int32_t nsplit = (int32_t)((blk + ksplit - 1) / ksplit);
@@ -343,8 +441,12 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     TBK_CUDA(cudaEventRecord(ev[0], st));
     if (kets) TBK_TRY(load_block_any(prec, n, R, r0, Rc, kstage.as<double2>(), v0, st));
     else TBK_TRY(random_block_any(prec, n, R, r0, Rc, seed, v0, st));
-    TBK_TRY(side(AL, BL, Ls.as<float2>()));
-    TBK_TRY(side(AR, BR, Rs.as<float2>()));
+    if (both) {
+      TBK_TRY(both_sides());
+    } else {
+      TBK_TRY(side(AL, BL, Ls.as<float2>()));
+      TBK_TRY(side(AR, BR, Rs.as<float2>()));
+    }
     TBK_CUDA(cudaEventRecord(ev[1], st));
     if (use_tc) {
       TBK_TRY(mu_gemm_tc(Ls.as<float2>(), Rs.as<float2>(), M, blk, macc.as<double>(), st));

@@ -123,6 +123,22 @@ int ensure_ell_dd(tbk_sparse_s* A, cudaStream_t st);   // double-float copy of t
 int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t st, int32_t* total_host);
 int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st, int64_t* total_host);
 int sm_count();
+// complex64 K-tiled stores written by a recursion step (Kubo blocks).  Element
+// k of block m sits at ((k / 16) * kM + m) * 16 + k % 16.  The step's columns
+// form `halves` groups (1 or 2) of R / halves columns; group h writes block
+// km[h] (none when negative) of store[h], k = row * (R / halves) + column in
+// the group, with either the step output or V x for its operator V (values
+// vval[h] / vdiag[h], same ELL structure as H; null: H's own values).
+struct KStore {
+  float2* store[2] = {nullptr, nullptr};
+  const void* vval[2] = {nullptr, nullptr};
+  const void* vdiag[2] = {nullptr, nullptr};
+  int32_t km[2] = {-1, -1};
+  int32_t usev[2] = {0, 0};
+  int32_t kM = 0;
+  int32_t halves = 1;
+};
+
 // kpm.cu — one fused recursion step with the one-pass kernel in a precision
 // TBK_PREC_* (complex64, complex128 or double-float vectors): y = H x (first)
 // or y = 2 H x - pv; moment partials into part[2 * grid].  Block loaders:
@@ -135,6 +151,13 @@ int step_config(tbk_sparse_s* A, int Rc, int prec, int* grid, int* n_tiles, cuda
 int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
              int grid, int n_tiles, cudaStream_t st, float2* kstore = nullptr, int32_t kM = 0, int32_t km = 0,
              bool store_y = true, tbk_sparse_s* vop = nullptr);
+// ELL value / diagonal arrays of a precision (FP32, FP64 or double-float pairs)
+const void* ell_vals(const EllDev& E, int prec);
+const void* ell_diag(const EllDev& E, int prec);
+// one recursion step (not the first block's braket form) writing the K-tiled
+// stores described by ks (output or operator products per column group)
+int step_ks(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
+            int grid, int n_tiles, cudaStream_t st, const KStore& ks);
 // true when B's sliced ELL has A's slices, widths and columns (values may differ)
 int same_ell_structure(tbk_sparse_s* A, tbk_sparse_s* B, bool* same, cudaStream_t st);
 int load_block_any(int prec, int32_t n, int32_t R, int32_t r0, int32_t Rp, const double2* src, void* dst,

@@ -28,12 +28,13 @@ _RECURSION = {"fp64": 0, "mixed": capi.MU_MIXED_RECURSION, "dd": capi.MU_DD_RECU
 
 def kubo_mu(Ht: SparseMatrix, AL=None, BL=None, AR=None, BR=None, M: int = 64, R: int = 4, seed: int = 0,
             kets=None, kernel: Kernel | None = None, tensor: bool = False, budget_gb: float = 0.0,
-            recursion: str = "dd", fuse_ops: bool = True) -> np.ndarray:
+            recursion: str = "dd", fuse_ops: bool = True, separate_sides: bool = False) -> np.ndarray:
     """mu_mn = sum conj(g_m AL T_m BL r) (g_n AR T_n BR r); operators None = identity.
     recursion: "dd" (default; double-float work blocks: FP64-class accuracy on the
     FP32 pipe), "fp64" (complex128) or "mixed" (complex64, FP32 H~).  fuse_ops:
     form AL / AR products inside the recursion step when they share H~'s
-    sparsity (same stored bits, one pass instead of two)."""
+    sparsity (same stored bits, one pass instead of two); with fused operators
+    both sides run as one recursion of twice the width unless separate_sides."""
     kernel = kernel if kernel is not None else Dirichlet()
     mu = np.zeros((M, M), dtype=np.complex128)
     K = None
@@ -43,7 +44,8 @@ def kubo_mu(Ht: SparseMatrix, AL=None, BL=None, AR=None, BR=None, M: int = 64, R
     check(lib().tbk_kubo_mu(Ht.handle, _h(AL), _h(BL), _h(AR), _h(BR), M, R, int(seed),
                             None if K is None else capi.ptr(K), kernel.kind, kernel.p0, kernel.p1,
                             (capi.MU_TENSOR if tensor else capi.MU_CUDA_CORE) | _RECURSION[recursion]
-                            | (0 if fuse_ops else capi.MU_UNFUSED_OPS),
+                            | (0 if fuse_ops else capi.MU_UNFUSED_OPS)
+                            | (capi.MU_SEPARATE_SIDES if separate_sides else 0),
                             float(budget_gb), capi.ptr(mu), None))
     return mu
 
