@@ -401,7 +401,7 @@ def peaks_tensor():
     return 1900.0 / 2.0, "half of fallback bf16"
 
 
-def run_kubo(config: int, tensor: bool = True, recursion: str = "dd", fuse_ops: bool = True, moments: int = 0,
+def run_kubo(config: int, tensor: bool = True, recursion: str = "dd", fuse_ops: bool = False, moments: int = 0,
              budget_gb: float = 0.0):
     """Kubo legs: config 3 (Bastin sigma_xy, square 256^2 open-x / periodic-y, Landau
     flux 1/64, M = 512, R = 16, seed 2) or config 5 (Greenwood sigma_xx, FCC 128^3
@@ -774,8 +774,8 @@ def main():
                     help="override M of the Kubo leg (small profiling case; not the benchmark)")
     ap.add_argument("--kubo-budget-gb", type=float, default=0.0,
                     help="stored-block budget of the Kubo leg (0: 60%% of free memory)")
-    ap.add_argument("--kubo-unfused", action="store_true",
-                    help="Kubo leg with the output-operator products in passes of their own (A/B)")
+    ap.add_argument("--kubo-fused", action="store_true",
+                    help="Kubo leg with the output-operator products fused into the recursion (A/B)")
     ap.add_argument("--no-hopping", action="store_true",
                     help="diagonal-only H (same vector streams, no neighbour gathers): stream ceiling")
     ap.add_argument("--serve", action="store_true", help="serving stream (config 4) instead of the DoS solve")
@@ -807,7 +807,7 @@ def main():
         return run_kernel_only(args)
     if args.kubo:
         print(json.dumps(run_kubo(args.kubo, tensor=not args.cuda_core_mu, recursion=args.kubo_recursion,
-                                  fuse_ops=not args.kubo_unfused, moments=args.kubo_moments,
+                                  fuse_ops=args.kubo_fused, moments=args.kubo_moments,
                                   budget_gb=args.kubo_budget_gb)), flush=True)
         return 0
     if args.impl == "reference":

@@ -318,12 +318,14 @@ enum {
   TBK_MU_MIXED_RECURSION = 2,       /* complex64 recursion for the stored blocks (FP32
                                        H~); default: complex128 recursion, FP64 H~      */
   TBK_MU_DD_RECURSION = 4,          /* double-float recursion for the stored blocks     */
-  TBK_MU_UNFUSED_OPS = 8,           /* apply the output operator in a pass of its own
-                                       (default: fused into the recursion step when it
-                                       shares H~'s sparsity, as commutators do)        */
-  TBK_MU_SEPARATE_SIDES = 16        /* run the left and right recursions one after the
-                                       other (default: as one recursion of twice the
-                                       width when the output operators fuse)           */
+  TBK_MU_FUSED_OPS = 8,             /* form the output operator's products inside the
+                                       recursion step when it shares H~'s sparsity (as
+                                       commutators do): same stored bits, one pass per
+                                       block instead of two; opt-in: the wider step holds
+                                       more registers and measured no faster            */
+  TBK_MU_BOTH_SIDES = 16            /* with TBK_MU_FUSED_OPS: run the left and right
+                                       recursions as one of twice the width (same bits;
+                                       opt-in, measured no faster)                      */
 };
 /* mu_mn = sum_{sites,r} conj(aL_m) aR_n with aL_m = g_m AL T_m(H~) BL |r>,
  * aR_n = g_n AR T_n(H~) BR |r> (NULL operator = identity), m, n < M: the stored

@@ -211,12 +211,12 @@ def test_fused_operator_products_same_bits(gpu, which, recursion):
     v_y = tb.commutator(Ht, X.op_position(1))
     kw = dict(M=48, R=4, seed=3, kernel=tb.Lorentz(6.0), tensor=True, recursion=recursion)
     if which == "bastin":
-        a = tb.kubo_mu(Ht, None, None, v_x, v_y, **kw)
-        b = tb.kubo_mu(Ht, None, None, v_x, v_y, fuse_ops=False, **kw)
-        c = tb.kubo_mu(Ht, None, None, v_x, v_y, separate_sides=True, **kw)
+        a = tb.kubo_mu(Ht, None, None, v_x, v_y, fuse_ops=True, **kw)
+        b = tb.kubo_mu(Ht, None, None, v_x, v_y, **kw)
+        c = tb.kubo_mu(Ht, None, None, v_x, v_y, fuse_ops=True, both_sides=True, **kw)
     else:
-        a = tb.kubo_mu(Ht, v_x, v_x, None, None, **kw)
-        b = tb.kubo_mu(Ht, v_x, v_x, None, None, fuse_ops=False, **kw)
-        c = tb.kubo_mu(Ht, v_x, v_x, None, None, separate_sides=True, **kw)
-    assert np.array_equal(a, b)      # both sides as one recursion vs separate passes
-    assert np.array_equal(a, c)      # vs separate sides with fused products
+        a = tb.kubo_mu(Ht, v_x, v_x, None, None, fuse_ops=True, **kw)
+        b = tb.kubo_mu(Ht, v_x, v_x, None, None, **kw)
+        c = tb.kubo_mu(Ht, v_x, v_x, None, None, fuse_ops=True, both_sides=True, **kw)
+    assert np.array_equal(a, b)      # fused products vs separate passes
+    assert np.array_equal(a, c)      # vs both sides as one recursion

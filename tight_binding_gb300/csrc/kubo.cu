@@ -282,10 +282,10 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   const int64_t blk16 = (blk + 15) / 16 * 16;           // K padded to whole 16-element tiles (zeros)
   TBK_TRY(Ls.alloc(sizeof(float2) * blk16 * M));
   TBK_TRY(Rs.alloc(sizeof(float2) * blk16 * M));
-  // both sides as one recursion of width 2 Rc when every output operator can
-  // be fused into the step (the gathers move twice the bytes per row; the
-  // stored values are the same bits)
-  bool both = !(flags & (TBK_MU_SEPARATE_SIDES | TBK_MU_UNFUSED_OPS)) &&
+  // both sides as one recursion of width 2 Rc (TBK_MU_BOTH_SIDES) when every
+  // output operator can be fused into the step (the gathers move twice the
+  // bytes per row; the stored values are the same bits)
+  bool both = (flags & TBK_MU_BOTH_SIDES) && (flags & TBK_MU_FUSED_OPS) &&
               2 * Rc <= (prec == TBK_PREC_MIXED ? 64 : 32) && (prec != TBK_PREC_MIXED || Rc >= 2);
   for (tbk_sparse_s* o : {AL, AR}) {
     if (!both || !o) continue;
@@ -340,15 +340,15 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   };
   // one side: store[m] = Aout T_m(H~) (Bin v0), m < M; each step writes its
   // complex64 block (Aout absent) or feeds the product that does
-  // With an output operator that shares H~'s ELL structure (a commutator
-  // [X, H~] does), step m also forms Aout T_{m-1} from the x it gathers and
-  // writes block m-1: one pass over the matrix and the vectors per block
-  // instead of two.  The stored values are the same bits either way.
+  // TBK_MU_FUSED_OPS: with an output operator that shares H~'s ELL structure
+  // (a commutator [X, H~] does), step m also forms Aout T_{m-1} from the x it
+  // gathers and writes block m-1: one pass over the matrix and the vectors per
+  // block instead of two.  The stored values are the same bits either way.
   auto side = [&](tbk_sparse_s* Aout, tbk_sparse_s* Bin, float2* store) -> int {
     void* r[3] = {wblk(0), wblk(1), wblk(2)};
     void* tmpA = wblk(3);
     bool fuse = false;
-    if (Aout && !(flags & TBK_MU_UNFUSED_OPS)) {
+    if (Aout && (flags & TBK_MU_FUSED_OPS)) {
       TBK_TRY(same_ell_structure(Ht, Aout, &fuse, st));
       if (fuse && prec == TBK_PREC_DD) TBK_TRY(ensure_ell_dd(Aout, st));
     }
