@@ -220,3 +220,27 @@ def test_fused_operator_products_same_bits(gpu, which, recursion):
         c = tb.kubo_mu(Ht, v_x, v_x, None, None, fuse_ops=True, both_sides=True, **kw)
     assert np.array_equal(a, b)      # fused products vs separate passes
     assert np.array_equal(a, c)      # vs both sides as one recursion
+
+
+def test_greenwood_mu_fcc_wide_rows(gpu):
+    """FCC (12 neighbours: pipelined gathers) Kubo-Greenwood mu_nm against the
+    oracle, and the fused / two-sided variants against the plain one."""
+    tb = gpu
+    X = tb.PartialLattice(tb.FCC().add_hopping("A", 1, 1.0), (8, 7, 6))
+    X.set_scalar_disorder(2.0, 4)
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1, 1], complex)
+    G = tb.GreenFunction(40, H, -13.0, 13.0)
+    Ht = G.scaled_HE
+    v_x = tb.commutator(Ht, X.op_position(0))
+    cp, ri, v = Ht.to_csc()
+    n = len(cp) - 1
+    xs = X.op_position(0).to_csc()[2]
+    ovx = (cp, ri, orc.commutator_values(n, cp, ri, v, xs))
+    kets = orc.random_phase_kets(n, 4, 6)
+    g = orc.kernel_seq(orc.K_LORENTZ, 40, 6.0)
+    kw = dict(M=40, kets=kets, kernel=tb.Lorentz(6.0), tensor=True)
+    mu = tb.kubo_mu(Ht, v_x, v_x, None, None, **kw)
+    ref = orc.kubo_mu(n, cp, ri, v, 40, kets, AL=ovx, BL=ovx, g=g)
+    assert _rel(mu, ref) <= MU_TOL, _rel(mu, ref)
+    assert np.array_equal(mu, tb.kubo_mu(Ht, v_x, v_x, None, None, fuse_ops=True, **kw))
+    assert np.array_equal(mu, tb.kubo_mu(Ht, v_x, v_x, None, None, fuse_ops=True, both_sides=True, **kw))

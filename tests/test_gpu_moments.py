@@ -274,3 +274,29 @@ def test_one_launch_recursion_matches_oracle(gpu, precision, doubling, cplx, R):
     tol = {"fp64": 1e-10, "dd": DD_TOL, "mixed": MIXED_TOL}[precision]
     assert np.max(np.abs(a - ref)) / abs(ref[0]) <= tol
     assert np.max(np.abs(a - b)) / abs(ref[0]) <= (1e-13 if precision != "mixed" else 1e-6)
+
+
+@pytest.mark.parametrize("precision,doubling", [("fp64", False), ("fp64", True), ("mixed", True), ("dd", False),
+                                                ("dd", True)])
+@pytest.mark.parametrize("case", ["fcc_disorder", "square_nn2_gauge"])
+def test_wide_rows_pipelined_gathers(gpu, precision, doubling, case):
+    """Rows wider than one group of 4 gathers (FCC: 12 neighbours; square with
+    first and second neighbours: 8) take the pipelined column loads."""
+    tb = gpu
+    if case == "fcc_disorder":
+        _, H = _system(tb, "fcc", (10, 9, 8), disorder=(2.0, 4))
+        a = 13.2
+    else:
+        cell = tb.Square().add_hopping("A", 1, 1.0).add_hopping("A", 2, 0.3)
+        X = tb.PartialLattice(cell, (20, 18))
+        X.set_gauge_linear(*landau_gauge(0.07))
+        H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], complex)
+        a = 5.4
+    G, cp, ri, v = _rescaled_csc(tb, H, a)
+    n = len(cp) - 1
+    kets = orc.random_phase_kets(n, 6, 2)
+    bras = kets if doubling else orc.random_phase_kets(n, 6, 3)
+    mu = tb.Cheb_first_kind_seq_braket((n, cp, ri, v), 80, bras, kets, precision=precision, doubling=doubling)
+    ref = orc.cheb_moments(n, cp, ri, v, 80, bras, kets)
+    tol = {"fp64": 1e-10, "dd": DD_TOL, "mixed": MIXED_TOL}[precision]
+    assert _err(mu, ref) <= tol

@@ -1,0 +1,281 @@
+// kpm_step.cuh — the one-pass recursion step kernel and its launch templates.
+// Instantiated per vector precision in kpm_step_f32.cu, kpm_step_f64.cu and
+// kpm_step_dd.cu (compiled in parallel); everything else calls
+// launch_step_prec / occupancy_prec.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "kpm_device.cuh"
+#include "tbk_internal.h"
+
+namespace tbk {
+
+constexpr int kStepThreads = 256;
+constexpr int kStepWarps = kStepThreads / 32;
+
+// One recursion step over all rows, x = v_s, y = v_{s-1} on entry.
+//   FIRST: y = H x                    else: y = 2 H x - y  (v_{s+1} over v_{s-1})
+//   doubling (BRAKET false): part[0] += <x|x>; part[1] += <x|y_in> (= <v_s|v_{s-1}>),
+//                            FIRST: part[1] += <x|H x> (= <v_0|v_1>)
+//   braket:                  part[0] += <b|v_{s+1}>;  FIRST also part[1] += <b|x>
+//   gather == 0: no product at all (the last doubling step only needs the dots).
+//   KST: also write complex64 K-tiled stores (Kubo blocks, KStore): 1 = the
+//   output into one store; 2 = per column group the output or V x for an
+//   operator V with H's ELL structure, formed from the same gathered x (the
+//   operator product of the previous block fused into the step), so that the
+//   two sides of a Kubo pair can run as one recursion of twice the width.  A
+//   template parameter because even an untaken runtime branch there costs the
+//   moments recursion ~8% of its bandwidth.
+//   PIPE: rows wider than one group of 4 gathers (ELL width > 4, e.g. FCC's
+//   12 neighbours) load the next group's columns while this group's gathers
+//   are in flight: 4 dependent memory round trips per 12-neighbour row instead
+//   of 6 (1.8x on the FCC Kubo recursion).  Narrow rows keep the plain loop,
+//   whose extra predicated loads would cost the honeycomb recursion 8%.
+template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET, int KST = 0, bool PIPE = false>
+__global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
+    int32_t n, int32_t n_tiles, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
+    const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
+    typename C2<F>::T* y, const typename C2<F>::T* pv, const typename C2<F>::T* __restrict__ bras,
+    double* __restrict__ part, int store, int reverse, int gather, int pf_dist, const KStore ks) {
+  using CT = typename C2<F>::T;
+  constexpr int VPL = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
+  constexpr int LPR = R / VPL;             // lanes per row
+  constexpr int RPW = 32 / LPR;            // rows per warp
+  constexpr int ROWS_PER_TILE = RPW * kStepWarps;
+  static_assert(LPR >= 1 && LPR <= 32 && (32 % LPR) == 0, "R out of range");
+  using Acc = F;                           // per-thread sums in the vector precision
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane % LPR;
+  Acc m0 = 0, m1 = 0;
+
+  for (int32_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const int32_t tile = reverse ? (n_tiles - 1 - t) : t;
+    if (pf_dist > 0 && threadIdx.x == 0) {
+      // bring the streams of the tile this CTA reaches pf_dist iterations later
+      // into L2 ahead of time: its own rows of v_n and v_{n-1} (and the bras)
+      const int32_t tf = t + pf_dist * (int32_t)gridDim.x;
+      if (tf < n_tiles) {
+        const int32_t tilef = reverse ? (n_tiles - 1 - tf) : tf;
+        const int64_t rf = (int64_t)tilef * ROWS_PER_TILE;
+        const int32_t nr = (int32_t)min((int64_t)ROWS_PER_TILE, (int64_t)n - rf);
+        if (nr > 0) {
+          const uint32_t vb = (uint32_t)nr * (uint32_t)(R * sizeof(CT));
+          if ((vb & 15u) == 0) {
+            bulk_prefetch_l2(x + rf * R, vb);
+            if (!FIRST) bulk_prefetch_l2(pv + rf * R, vb);
+            if (BRAKET) bulk_prefetch_l2(bras + rf * R, vb);
+          }
+        }
+      }
+    }
+    const int32_t r = tile * ROWS_PER_TILE + warp * RPW + lane / LPR;
+    if (r >= n) continue;
+    const int64_t me = (int64_t)r * LPR + sub;
+    const LaneV<F, VPL> xs = ld_ro<F, VPL>(x + me * VPL);
+    LaneV<F, VPL> prev;
+    if constexpr (!FIRST) prev = ld_stream<F, VPL>(pv + me * VPL);   // pv == y: in place
+    LaneV<F, VPL> acc, vacc;
+#pragma unroll
+    for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
+    // column group of this lane (its VPL columns never straddle two groups)
+    const int grp = (KST == 2 && ks.halves == 2 && sub * VPL >= R / 2) ? 1 : 0;
+    const F* vval = nullptr;
+    const F* vdiag = nullptr;
+    if constexpr (KST == 2) {
+      const void* vv = grp ? ks.vval[1] : ks.vval[0];      // selects, not an indexed parameter array
+      const void* vd = grp ? ks.vdiag[1] : ks.vdiag[0];
+      vval = vv ? static_cast<const F*>(vv) : eval;
+      vdiag = vd ? static_cast<const F*>(vd) : diag;
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) { vacc.re[q] = 0; vacc.im[q] = 0; }
+    }
+    if (gather) {
+      HVal<F, CPLX_H>::load(diag, r).template fma<VPL>(xs, acc);
+      if constexpr (KST == 2) HVal<F, CPLX_H>::load(vdiag, r).template fma<VPL>(xs, vacc);
+      const int32_t s = r >> 5, l = r & 31;
+      const int32_t off = soff[s];
+      const int32_t w = (soff[s + 1] - off) >> 5;
+      const int32_t* cp = ecol + off + l;
+      // all of a row's gathers in flight together: predicated groups of 4
+      int32_t cn[4];
+      if constexpr (PIPE) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) cn[u] = u < w ? __ldg(cp + u * 32) : r;
+      }
+      for (int k = 0; k < w; k += 4) {
+        int32_t c[4];
+        HVal<F, CPLX_H> h[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const bool v = k + u < w;
+          if constexpr (PIPE) c[u] = cn[u];
+          else c[u] = v ? __ldg(cp + (k + u) * 32) : r;             // padding: own row
+          h[u] = v ? HVal<F, CPLX_H>::load(eval, off + l + (int64_t)(k + u) * 32) : HVal<F, CPLX_H>::zero();
+        }
+        if constexpr (PIPE) {                                       // next group's columns
+#pragma unroll
+          for (int u = 0; u < 4; ++u) cn[u] = k + 4 + u < w ? __ldg(cp + (k + 4 + u) * 32) : r;
+        }
+        LaneV<F, VPL> xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) xv[u] = ld_ro<F, VPL>(x + ((int64_t)c[u] * LPR + sub) * VPL);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
+        if constexpr (KST == 2) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const HVal<F, CPLX_H> hv = k + u < w ? HVal<F, CPLX_H>::load(vval, off + l + (int64_t)(k + u) * 32)
+                                                 : HVal<F, CPLX_H>::zero();
+            hv.template fma<VPL>(xv[u], vacc);
+          }
+        }
+      }
+    }
+    finish_acc<F, VPL>(acc);
+    if constexpr (KST == 2) finish_acc<F, VPL>(vacc);
+    LaneV<F, VPL> out;
+#pragma unroll
+    for (int q = 0; q < VPL; ++q) {
+      if constexpr (FIRST) { out.re[q] = acc.re[q]; out.im[q] = acc.im[q]; }
+      else { out.re[q] = F(2) * acc.re[q] - prev.re[q]; out.im[q] = F(2) * acc.im[q] - prev.im[q]; }
+    }
+    // moment partial sums (before the store, from registers only)
+    if constexpr (BRAKET) {
+      const LaneV<F, VPL> b = ld_ro<F, VPL>(bras + me * VPL);
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) {
+        m0 += b.re[q] * out.re[q] + b.im[q] * out.im[q];
+        if constexpr (FIRST) m1 += b.re[q] * xs.re[q] + b.im[q] * xs.im[q];
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) {
+        m0 += xs.re[q] * xs.re[q] + xs.im[q] * xs.im[q];
+        if constexpr (FIRST) m1 += xs.re[q] * out.re[q] + xs.im[q] * out.im[q];
+        else m1 += xs.re[q] * prev.re[q] + xs.im[q] * prev.im[q];
+      }
+    }
+    if (store) st_v<F, VPL>(y + me * VPL, out);
+    if constexpr (KST == 1) {
+      // block km[0] of the K-tiled store: one rounding per value
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) {
+        const int64_t k = (int64_t)r * R + sub * VPL + q;
+        ks.store[0][((k >> 4) * ks.kM + ks.km[0]) * 16 + (k & 15)] = make_float2(to_f32(out.re[q]), to_f32(out.im[q]));
+      }
+    } else if constexpr (KST == 2) {
+      const int32_t kmg = grp ? ks.km[1] : ks.km[0];
+      if (kmg >= 0) {
+        const int32_t Rg = R / ks.halves;
+        const LaneV<F, VPL>& sv = (grp ? ks.usev[1] : ks.usev[0]) ? vacc : out;
+        float2* dst = grp ? ks.store[1] : ks.store[0];
+#pragma unroll
+        for (int q = 0; q < VPL; ++q) {
+          const int64_t k = (int64_t)r * Rg + sub * VPL + q - grp * Rg;
+          dst[((k >> 4) * ks.kM + kmg) * 16 + (k & 15)] = make_float2(to_f32(sv.re[q]), to_f32(sv.im[q]));
+        }
+      }
+    }
+  }
+  // FP64 from here on: warp shuffle, then across the CTA's warps
+  double d0 = (double)m0, d1 = (double)m1;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    d0 += __shfl_xor_sync(0xffffffffu, d0, o);
+    d1 += __shfl_xor_sync(0xffffffffu, d1, o);
+  }
+  __shared__ double sh[2][kStepWarps];
+  if (lane == 0) { sh[0][warp] = d0; sh[1][warp] = d1; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+#pragma unroll
+    for (int q = 0; q < kStepWarps; ++q) { a += sh[0][q]; b += sh[1][q]; }
+    part[blockIdx.x] = a;
+    part[gridDim.x + blockIdx.x] = b;
+  }
+}
+
+
+// ----------------------------------------------------------------- dispatch
+struct StepArgs {
+  int32_t n, n_tiles, n_slices;
+  int* err;
+  const int32_t* soff;
+  const int32_t* ecol;
+  const void* eval;
+  const void* diag;
+  const void* x;
+  void* y;
+  const void* pv;      // v_{n-1}; equal to y for the in-place recursion
+  const void* bras;
+  double* part;
+  int store, reverse, gather, pf_dist;
+  KStore ks;                   // optional complex64 K-tiled stores (Kubo blocks)
+  int kst = 0;                 // 0 none, 1 output into ks.store[0], 2 per-group output / V x
+  bool pipe = false;           // ELL wider than 4: pipelined column loads
+};
+
+template <typename F, int R, bool CPLX_H>
+inline int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, cudaStream_t st) {
+  using CT = typename C2<F>::T;
+  auto x = static_cast<const CT*>(a.x);
+  auto y = static_cast<CT*>(a.y);
+  auto pv = static_cast<const CT*>(a.pv ? a.pv : a.y);
+  auto b = static_cast<const CT*>(a.bras);
+  auto ev = static_cast<const F*>(a.eval);
+  auto dg = static_cast<const F*>(a.diag);
+#define TBK_STEP(FI, BR, KS)                                                                          \
+  do {                                                                                                \
+    if (a.pipe)                                                                                       \
+      kpm_step_kernel<F, R, CPLX_H, FI, BR, KS, true><<<grid, kStepThreads, 0, st>>>(                 \
+          a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.ks); \
+    else                                                                                              \
+      kpm_step_kernel<F, R, CPLX_H, FI, BR, KS, false><<<grid, kStepThreads, 0, st>>>(                \
+          a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.ks); \
+  } while (0)
+  if (a.kst != 0) {
+    if (braket) return fail(TBK_ERR_UNSUPPORTED, "K-tiled store with a braket step");
+    constexpr int VPLR = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
+    if (a.kst == 2 && a.ks.halves == 2 && (R / 2) % VPLR != 0)
+      return fail(TBK_ERR_UNSUPPORTED, "column groups narrower than a lane's vectors");
+    if (a.kst == 2) { if (first) TBK_STEP(true, false, 2); else TBK_STEP(false, false, 2); }
+    else { if (first) TBK_STEP(true, false, 1); else TBK_STEP(false, false, 1); }
+  } else if (first) { if (braket) TBK_STEP(true, true, 0); else TBK_STEP(true, false, 0); }
+  else { if (braket) TBK_STEP(false, true, 0); else TBK_STEP(false, false, 0); }
+#undef TBK_STEP
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
+}
+
+template <typename F, bool CPLX_H>
+inline int launch_step(int R, const StepArgs& a, bool first, bool braket, int grid, cudaStream_t st) {
+  switch (R) {
+    case 1: return launch_step_r<F, 1, CPLX_H>(a, first, braket, grid, st);
+    case 2: return launch_step_r<F, 2, CPLX_H>(a, first, braket, grid, st);
+    case 4: return launch_step_r<F, 4, CPLX_H>(a, first, braket, grid, st);
+    case 8: return launch_step_r<F, 8, CPLX_H>(a, first, braket, grid, st);
+    case 16: return launch_step_r<F, 16, CPLX_H>(a, first, braket, grid, st);
+    case 32: return launch_step_r<F, 32, CPLX_H>(a, first, braket, grid, st);
+    case 64:
+      if constexpr (sizeof(F) == 4) return launch_step_r<F, 64, CPLX_H>(a, first, braket, grid, st);
+      break;
+  }
+  return fail(TBK_ERR_UNSUPPORTED, "chunk width %d not instantiated", R);
+}
+
+
+template <typename F, bool CPLX_H, int R>
+inline int occupancy_blocks() {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kpm_step_kernel<F, R, CPLX_H, false, false, 0, false>, kStepThreads, 0);
+  return nb > 0 ? nb : 1;
+}
+
+// per-precision entry points (TBK_PREC_*)
+int launch_step_prec(int prec, bool cplx, int R, const StepArgs& a, bool first, bool braket, int grid,
+                     cudaStream_t st);
+int occupancy_prec(int prec, bool cplx, int R);
+
+}  // namespace tbk
