@@ -144,3 +144,20 @@ def test_expansion_coefficients_host(tb):
         assert np.max(np.abs(c - ref)) <= 1e-14
         assert abs(special.jv(len(c), a * t)) < 1e-15
     assert tb.evolution_terms(1.0, 100.0) > 100
+
+
+def test_new_entry_points_reject_bad_arguments_without_gpu(tb):
+    """Argument checks of the spectral-range, expansion and moment-file entry
+    points run before any device work (CPU-only)."""
+    import ctypes as C
+    from tight_binding_gb300 import capi
+    L = capi.lib()
+    d = C.c_double()
+    assert L.tbk_spectral_range(None, 10, 0, C.byref(d), C.byref(d), None, None, None) == capi.TBK_ERR_INVALID
+    assert b"null argument" in L.tbk_last_error()
+    assert L.tbk_cheb_expand(None, 4, None, 1, None, None, 0, None) == capi.TBK_ERR_INVALID
+    assert L.tbk_cheb_coef_delta(0.1, -1, None) == capi.TBK_ERR_INVALID
+    assert L.tbk_cheb_coef_evolution(1.0, 0.0, 1.0, 0, None) == capi.TBK_ERR_INVALID
+    k = C.c_int32()
+    assert L.tbk_cheb_evolution_terms(1.0, 1.0, 0.0, C.byref(k)) == capi.TBK_ERR_INVALID
+    assert L.tbk_moments_save(None, None, None) == capi.TBK_ERR_INVALID
