@@ -441,6 +441,10 @@ def run_kubo(config: int, tensor: bool = True, recursion: str = "dd", fuse_ops: 
             "gemm_tflops_useful": useful / (tmg["ms_gemm"] / 1e3) / 1e12,
             "tensor_peak_tflops": peak, "tensor_peak_source": src,
             "blocks_GBps": tmg["block_bytes"] / (tmg["ms_blocks"] / 1e3) / 1e9, **result}
+    hbm, hbm_src = peaks()
+    line["blocks_roofline"] = {"bound": "hbm", "achieved": line["blocks_GBps"], "peak": hbm, "unit": "GB/s",
+                               "frac": line["blocks_GBps"] / hbm, "peak_source": hbm_src,
+                               "bytes": "algorithmic: work vectors + matrix per pass + complex64 stores"}
     if tensor:
         line["tensor_util"] = line["gemm_tflops_issued"] / peak
     return line

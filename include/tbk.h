@@ -343,7 +343,8 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
 /* Device time of the last tbk_kubo_mu call in this process (CUDA events on its
  * stream): building the stored blocks, the mu GEMM (+ split-K reduction), the
  * real flops of the GEMM products issued (3 split-TF32 terms on the tensor
- * path), the bytes of stored blocks written, and the number of vector chunks. */
+ * path), the algorithmic DRAM bytes of the block phase (work vectors read and
+ * written, matrix per pass, complex64 stores), and the number of vector chunks. */
 int tbk_kubo_last_timing(double* ms_blocks, double* ms_gemm, double* gemm_flops, double* block_bytes,
                          int32_t* chunks);
 /* mu_mn = sum_k conj(L_m[k]) R_n[k] for given blocks (host, M x K complex128

@@ -319,12 +319,23 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   char* wb = work.as<char>();
   auto wblk = [&](int i) { return static_cast<void*>(wb + (size_t)i * blk * csz); };
   void* v0 = wblk(5);
+  // algorithmic DRAM bytes of the block phase: vector blocks read / written,
+  // matrix (ELL columns + values + diagonal) per pass, complex64 stores
+  double rec_bytes = 0.0;
+  const double vecb = (double)blk * csz, stb = (double)blk * 8.0;
+  const int vsz = prec == TBK_PREC_MIXED ? 4 : 8;
+  auto ell_bytes = [&](tbk_sparse_s* A, bool cols) {
+    const double hv = (double)vsz * (A->ell.cplx ? 2 : 1);
+    return (double)A->ell.n_entries * ((cols ? 4.0 : 0.0) + hv) + (double)A->rows * hv;
+  };
   auto apply = [&](tbk_sparse_s* A, const void* x, void* y) -> int {   // y = A x
+    rec_bytes += 2 * vecb + ell_bytes(A, true);
     int g, t;
     TBK_TRY(step_config(A, Rc, prec, &g, &t, st));
     return step_any(A, Rc, prec, x, y, nullptr, true, partd.as<double>(), g, t, st);
   };
   auto round_to = [&](const void* src, float2* store, int32_t m) -> int {
+    rec_bytes += vecb + stb;
     const unsigned g = (unsigned)std::min<int64_t>((blk + 255) / 256, 65535);
     if (prec == TBK_PREC_FP64) round_block_kernel<double2><<<g, 256, 0, st>>>(static_cast<const double2*>(src), store, m, M, blk);
     else if (prec == TBK_PREC_DD) round_block_kernel<dd2><<<g, 256, 0, st>>>(static_cast<const dd2*>(src), store, m, M, blk);
@@ -334,6 +345,7 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   };
   // block m of `store` = A x, written by the product itself (no work block)
   auto apply_to_store = [&](tbk_sparse_s* A, const void* x, void* scratch, float2* store, int32_t m) -> int {
+    rec_bytes += vecb + ell_bytes(A, true) + stb;
     int g, t;
     TBK_TRY(step_config(A, Rc, prec, &g, &t, st));
     return step_any(A, Rc, prec, x, scratch, nullptr, true, partd.as<double>(), g, t, st, store, M, m, false);
@@ -359,6 +371,8 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
       if (m >= 1) {
         const void* x = r[(m - 1) % 3];
         const void* pv = m >= 2 ? r[(m - 2) % 3] : nullptr;
+        rec_bytes += (m >= 2 ? 3 : 2) * vecb + ell_bytes(Ht, true) + ((fuse || !Aout) ? stb : 0.0) +
+                     (fuse ? ell_bytes(Aout, false) : 0.0);
         if (fuse)
           TBK_TRY(step_any(Ht, Rc, prec, x, y, pv, m == 1, partd.as<double>(), grid, n_tiles, st, store, M, m - 1,
                            true, Aout));
@@ -418,7 +432,11 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
       ks.vval[h] = Aout[h] ? ell_vals(Aout[h]->ell, prec) : nullptr;
       ks.vdiag[h] = Aout[h] ? ell_diag(Aout[h]->ell, prec) : nullptr;
     }
+    rec_bytes += 2 * (vecb + 2 * vecb);                  // start halves packed into the wide block
+    for (int h = 0; h < 2; ++h) rec_bytes += Aout[h] ? 0.0 : 2 * vecb + stb;
     for (int32_t m = 1; m < M; ++m) {
+      rec_bytes += 2 * (m >= 2 ? 3 : 2) * vecb + ell_bytes(Ht, true) + 2 * stb;
+      for (int h = 0; h < 2; ++h) rec_bytes += Aout[h] ? ell_bytes(Aout[h], false) : 0.0;
       for (int h = 0; h < 2; ++h) ks.km[h] = Aout[h] ? m - 1 : m;
       TBK_TRY(step_ks(Ht, 2 * Rc, prec, r[(m - 1) % 3], r[m % 3], m >= 2 ? r[(m - 2) % 3] : nullptr, m == 1,
                       partd.as<double>(), grid2, tiles2, st, ks));
@@ -466,7 +484,8 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     tm.ms_blocks += a;
     tm.ms_gemm += b;
     tm.gemm_flops += 8.0 * M * (double)M * (double)blk * (use_tc ? 3.0 : 1.0);   // real flops of the products issued
-    tm.block_bytes += 2.0 * M * (double)blk * 8.0;
+    tm.block_bytes += rec_bytes;
+    rec_bytes = 0.0;
     tm.chunks += 1;
   }
   for (auto& e : ev) cudaEventDestroy(e);
