@@ -408,35 +408,43 @@ def run_kubo(config: int, tensor: bool = True, recursion: str = "dd", fuse_ops: 
     periodic, on-site U[-1,1] seed 4, M = 1024, R = 8)."""
     import tight_binding_gb300 as tb
 
-    t0 = time.perf_counter()
-    if config == 3:
-        L, M, R = 256, moments or 512, 16
-        X = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (L, L))
-        G = np.zeros((3, 3))
-        G[1, 0] = 2 * np.pi / 64
-        X.set_gauge_linear(G, np.zeros(3))
-        H = X.get_Hamiltonian_periodic_extend_bare_sparse([0, 1], complex)
-        out = tb.conductivity_Kubo_Bastin(H, X.op_position(0), X.op_position(1), M, -4.0, 4.0, R=R, seed=2,
-                                          tensor=tensor, recursion=recursion, fuse_ops=fuse_ops, budget_gb=budget_gb)
-        result = {"E_F_points": int(len(out["E"])), "sigma_xy_at_E0": float(out["sigma_re"][len(out["E"]) // 2])}
-        workload = "Kubo-Bastin sigma_xy: square 256x256 open-x/periodic-y, Landau flux 1/64, M=512, R=16 seed 2"
-    else:
-        L, M, R = 128, moments or 1024, 8
-        X = tb.PartialLattice(tb.FCC().add_hopping("A", 1, 1.0), (L, L, L))
-        X.set_scalar_disorder(2.0, 4)
-        H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1, 1], complex)
-        eps, sigma, mu = tb.conductivity_spectrum(H, X.op_position(0), X.op_position(1), M, R=R, seed=4,
-                                                  E_min=-13.0, E_max=13.0, tensor=tensor, recursion=recursion,
-                                                  fuse_ops=fuse_ops, budget_gb=budget_gb)
-        result = {"energies": int(len(eps)), "sigma_xx_max": float(np.max(sigma))}
-        workload = "Kubo-Greenwood sigma_xx: FCC 128^3 periodic, disorder U[-1,1] seed 4, M=1024, R=8"
-    wall = time.perf_counter() - t0
+    def once():
+        t0 = time.perf_counter()
+        if config == 3:
+            L, M, R = 256, moments or 512, 16
+            X = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (L, L))
+            G = np.zeros((3, 3))
+            G[1, 0] = 2 * np.pi / 64
+            X.set_gauge_linear(G, np.zeros(3))
+            H = X.get_Hamiltonian_periodic_extend_bare_sparse([0, 1], complex)
+            out = tb.conductivity_Kubo_Bastin(H, X.op_position(0), X.op_position(1), M, -4.0, 4.0, R=R, seed=2,
+                                              tensor=tensor, recursion=recursion, fuse_ops=fuse_ops, budget_gb=budget_gb)
+            result = {"E_F_points": int(len(out["E"])), "sigma_xy_at_E0": float(out["sigma_re"][len(out["E"]) // 2])}
+            workload = "Kubo-Bastin sigma_xy: square 256x256 open-x/periodic-y, Landau flux 1/64, M=512, R=16 seed 2"
+        else:
+            L, M, R = 128, moments or 1024, 8
+            X = tb.PartialLattice(tb.FCC().add_hopping("A", 1, 1.0), (L, L, L))
+            X.set_scalar_disorder(2.0, 4)
+            H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1, 1], complex)
+            eps, sigma, mu = tb.conductivity_spectrum(H, X.op_position(0), X.op_position(1), M, R=R, seed=4,
+                                                      E_min=-13.0, E_max=13.0, tensor=tensor, recursion=recursion,
+                                                      fuse_ops=fuse_ops, budget_gb=budget_gb)
+            result = {"energies": int(len(eps)), "sigma_xx_max": float(np.max(sigma))}
+            workload = "Kubo-Greenwood sigma_xx: FCC 128^3 periodic, disorder U[-1,1] seed 4, M=1024, R=8"
+        return time.perf_counter() - t0, workload, result
+
+    # the first call includes CUDA context creation and module loading; the
+    # second is the steady-state cost of a solve
+    wall_cold, workload, result = once()
+    wall, workload, result = once()
+
     tmg = tb.kubo_last_timing()
     peak, src = peaks_tensor()
     useful = tmg["gemm_flops"] / (3.0 if tensor else 1.0)       # one complex GEMM = 8 M^2 K real flops
     line = {"workload": workload, "path": "tcgen05 3xTF32" if tensor else "CUDA-core FP32", "recursion": recursion,
-            "fused_operator_products": fuse_ops, "moments": M,
-            "wall_s": wall, "blocks_ms": tmg["ms_blocks"], "gemm_ms": tmg["ms_gemm"], "chunks": tmg["chunks"],
+            "fused_operator_products": fuse_ops, "moments": moments or (512 if config == 3 else 1024),
+            "wall_s": wall, "wall_cold_s": wall_cold, "blocks_ms": tmg["ms_blocks"], "gemm_ms": tmg["ms_gemm"],
+            "chunks": tmg["chunks"],
             "gemm_tflops_issued": tmg["gemm_flops"] / (tmg["ms_gemm"] / 1e3) / 1e12,
             "gemm_tflops_useful": useful / (tmg["ms_gemm"] / 1e3) / 1e12,
             "tensor_peak_tflops": peak, "tensor_peak_source": src,
