@@ -83,3 +83,22 @@ def test_spectral_range_large_lattice_moments_bounded(gpu):
     G = tb.GreenFunction(256, H)
     mu = tb.KpmSolver(G.scaled_HE, 4, precision="fp64", doubling=True).run_random(256, seed=3)
     assert np.all(np.isfinite(mu)) and np.max(np.abs(mu)) <= abs(mu[0]) * (1 + 1e-9)
+
+
+def test_spectral_range_against_sparse_eigensolver(gpu):
+    """40,000-site disordered square lattice (past the reference's 5,000-row
+    Spectra cap): Lanczos extremes against ARPACK (scipy eigsh) on the same
+    CSC, and Ritz values inside the spectrum."""
+    tb = gpu
+    sla = pytest.importorskip("scipy.sparse.linalg")
+    sp = pytest.importorskip("scipy.sparse")
+    X = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (200, 200))
+    X.set_scalar_disorder(1.5, 8)
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], float)
+    cp, ri, v = H.to_csc()
+    n = len(cp) - 1
+    A = sp.csc_matrix((v.real if np.iscomplexobj(v) else v, ri, cp), shape=(n, n))
+    lo = sla.eigsh(A, k=1, which="SA", tol=1e-12, return_eigenvectors=False)[0]
+    hi = sla.eigsh(A, k=1, which="LA", tol=1e-12, return_eigenvectors=False)[0]
+    e0, e1, r0, r1 = tb.spectral_range(H, iters=600, seed=4)
+    assert lo - 1e-9 <= e0 <= lo + 1e-5 and hi - 1e-5 <= e1 <= hi + 1e-9, (e0, lo, e1, hi)
