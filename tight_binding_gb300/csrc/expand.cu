@@ -5,12 +5,17 @@
 // The reference walks T_n(H~)|k> with Cheb_first_kind_seq_view
 // (TB/numerical.h:346-361) and accumulates c_n T_n(H~)|k> on the host, e.g. the
 // single-energy delta projection of conductivity_test_sawtooth
-// (TB/snippets.h:173-223, c_n = a_d(n) T_n(e), n = 0 .. N).  Here the three-term
-// recursion runs with the one-pass step kernel on site-major work blocks (any
-// precision), and every step adds c_n T_n|k> into a complex128 accumulator in
-// the same layout; the accumulator is transposed back to Eigen's column-major
-// layout once per chunk of vectors.  Coefficient helpers: the delta projection
-// above and the time-evolution operator exp(-i H t) (Jacobi-Anger expansion).
+// (TB/snippets.h:173-223, c_n = a_d(n) T_n(e), n = 0 .. N).  Here the sum is
+// formed by Clenshaw's recurrence (Clenshaw, Math. Comp. 9, 1955) run
+// backwards over the coefficients on site-major work blocks:
+//   b_N = 0,  b_{N-1} = c_{N-1} v,  b_k = 2 H~ b_{k+1} - b_{k+2} + c_k v,
+//   out = (b_0 - b_2 + c_0 v) / 2,
+// each b_k by one pass of the step kernel with the c_k v term fused into it
+// (read v, x = b_{k+1}, b_{k+2}; write b_k in place), so no accumulator block
+// is read and written per term.  The result is converted to complex128 and
+// transposed back to Eigen's column-major layout once per chunk of vectors.
+// Coefficient helpers: the delta projection above and the time-evolution
+// operator exp(-i H t) (Jacobi-Anger expansion).
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -26,16 +31,28 @@ __device__ __forceinline__ double2 as_c128(float2 v) { return make_double2((doub
 __device__ __forceinline__ double2 as_c128(double2 v) { return v; }
 __device__ __forceinline__ double2 as_c128(dd2 v) { return make_double2((double)v.x, (double)v.y); }
 
-// acc (+)= c * v over cnt site-major elements
+// out = c v (work precision)
 template <typename F>
-__global__ void expand_axpy_kernel(int64_t cnt, const typename C2<F>::T* __restrict__ v, double cr, double ci,
-                                   double2* __restrict__ acc, int init) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += (int64_t)gridDim.x * blockDim.x) {
-    const double2 x = as_c128(v[i]);
-    double2 a = init ? make_double2(0.0, 0.0) : acc[i];
-    a.x = fma(cr, x.x, fma(-ci, x.y, a.x));
-    a.y = fma(cr, x.y, fma(ci, x.x, a.y));
-    acc[i] = a;
+__global__ void scale_block_kernel(int64_t cnt, const typename C2<F>::T* __restrict__ v, double cr, double ci,
+                                   typename C2<F>::T* __restrict__ out) {
+  const F r = F(cr), i = F(ci);
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += (int64_t)gridDim.x * blockDim.x) {
+    const typename C2<F>::T a = v[q];
+    typename C2<F>::T o;
+    o.x = r * a.x - i * a.y;
+    o.y = r * a.y + i * a.x;
+    out[q] = o;
+  }
+}
+
+// acc = (b0 - b2 + c0 v) / 2 in complex128
+template <typename F>
+__global__ void clenshaw_final_kernel(int64_t cnt, const typename C2<F>::T* __restrict__ b0,
+                                      const typename C2<F>::T* __restrict__ b2, const typename C2<F>::T* __restrict__ v,
+                                      double cr, double ci, double2* __restrict__ acc) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += (int64_t)gridDim.x * blockDim.x) {
+    const double2 a = as_c128(b0[q]), b = as_c128(b2[q]), x = as_c128(v[q]);
+    acc[q] = make_double2(0.5 * (a.x - b.x + (cr * x.x - ci * x.y)), 0.5 * (a.y - b.y + (cr * x.y + ci * x.x)));
   }
 }
 
@@ -63,18 +80,34 @@ int chunk_width(int prec, int32_t R) {
   return w;
 }
 
-template <typename F>
-int axpy(int64_t cnt, const void* v, double2 c, double2* acc, bool init, cudaStream_t st) {
-  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((cnt + 255) / 256, 8 * sm_count()));
-  expand_axpy_kernel<F><<<g, 256, 0, st>>>(cnt, static_cast<const typename C2<F>::T*>(v), c.x, c.y, acc, init ? 1 : 0);
+int grid_for(int64_t cnt) { return (int)std::max<int64_t>(1, std::min<int64_t>((cnt + 255) / 256, 8 * sm_count())); }
+
+int scale_any(int prec, int64_t cnt, const void* v, double2 c, void* out, cudaStream_t st) {
+  const int g = grid_for(cnt);
+  if (prec == TBK_PREC_FP64)
+    scale_block_kernel<double><<<g, 256, 0, st>>>(cnt, static_cast<const double2*>(v), c.x, c.y, static_cast<double2*>(out));
+  else if (prec == TBK_PREC_DD)
+    scale_block_kernel<dd><<<g, 256, 0, st>>>(cnt, static_cast<const dd2*>(v), c.x, c.y, static_cast<dd2*>(out));
+  else
+    scale_block_kernel<float><<<g, 256, 0, st>>>(cnt, static_cast<const float2*>(v), c.x, c.y, static_cast<float2*>(out));
   TBK_CHECK_LAUNCH();
   return TBK_OK;
 }
 
-int axpy_any(int prec, int64_t cnt, const void* v, double2 c, double2* acc, bool init, cudaStream_t st) {
-  if (prec == TBK_PREC_FP64) return axpy<double>(cnt, v, c, acc, init, st);
-  if (prec == TBK_PREC_DD) return axpy<dd>(cnt, v, c, acc, init, st);
-  return axpy<float>(cnt, v, c, acc, init, st);
+int final_any(int prec, int64_t cnt, const void* b0, const void* b2, const void* v, double2 c, double2* acc,
+              cudaStream_t st) {
+  const int g = grid_for(cnt);
+  if (prec == TBK_PREC_FP64)
+    clenshaw_final_kernel<double><<<g, 256, 0, st>>>(cnt, static_cast<const double2*>(b0), static_cast<const double2*>(b2),
+                                                     static_cast<const double2*>(v), c.x, c.y, acc);
+  else if (prec == TBK_PREC_DD)
+    clenshaw_final_kernel<dd><<<g, 256, 0, st>>>(cnt, static_cast<const dd2*>(b0), static_cast<const dd2*>(b2),
+                                                 static_cast<const dd2*>(v), c.x, c.y, acc);
+  else
+    clenshaw_final_kernel<float><<<g, 256, 0, st>>>(cnt, static_cast<const float2*>(b0), static_cast<const float2*>(b2),
+                                                    static_cast<const float2*>(v), c.x, c.y, acc);
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
 }
 
 }  // namespace
@@ -100,31 +133,40 @@ int tbk_cheb_expand(tbk_sparse Ht, int32_t n_terms, const double* coef, int32_t 
   const int64_t n_pad = (int64_t)Ht->ell.n_slices * 32;
   const size_t csz = prec == TBK_PREC_MIXED ? sizeof(float2) : prec == TBK_PREC_DD ? sizeof(dd2) : sizeof(double2);
   const int64_t cnt = n_pad * Rc;
-  DevBuf src, dst, va, vb, acc, part;
+  DevBuf src, dst, vk, ba, bb, bc, acc, part;
   TBK_TRY(src.alloc(sizeof(double2) * (size_t)n * R));
   TBK_TRY(dst.alloc(sizeof(double2) * (size_t)n * R));
-  TBK_TRY(va.alloc(csz * cnt));
-  TBK_TRY(vb.alloc(csz * cnt));
+  for (DevBuf* b : {&vk, &ba, &bb, &bc}) TBK_TRY(b->alloc(csz * cnt));
   TBK_TRY(acc.alloc(sizeof(double2) * cnt));
   TBK_TRY(part.alloc(sizeof(double) * 2 * grid));
   TBK_CUDA(cudaMemcpyAsync(src.p, kets, sizeof(double2) * (size_t)n * R, cudaMemcpyHostToDevice, st));
-  TBK_CUDA(cudaMemsetAsync(va.p, 0, va.bytes, st));
-  TBK_CUDA(cudaMemsetAsync(vb.p, 0, vb.bytes, st));
+  TBK_CUDA(cudaMemsetAsync(vk.p, 0, vk.bytes, st));
+  TBK_CUDA(cudaMemsetAsync(bc.p, 0, bc.bytes, st));                         // padding rows stay zero
   auto c_of = [&](int32_t k) { return make_double2(coef[2 * k], coef[2 * k + 1]); };
   for (int32_t r0 = 0; r0 < R; r0 += Rc) {
-    void* v_prev = va.p;     // T_{k-1}|k>
-    void* v_cur = vb.p;      // T_k|k>
-    TBK_TRY(load_block_any(prec, n, R, r0, Rc, src.as<double2>(), v_prev, st));
-    TBK_TRY(axpy_any(prec, cnt, v_prev, c_of(0), acc.as<double2>(), true, st));
-    if (n_terms > 1) {
-      TBK_TRY(step_any(Ht, Rc, prec, v_prev, v_cur, nullptr, true, part.as<double>(), grid, n_tiles, st));
-      TBK_TRY(axpy_any(prec, cnt, v_cur, c_of(1), acc.as<double2>(), false, st));
+    TBK_TRY(load_block_any(prec, n, R, r0, Rc, src.as<double2>(), vk.p, st));
+    // Clenshaw: x = b_{k+1}, p = b_{k+2}; b_k is written over p
+    void* p = ba.p;
+    void* x = bb.p;
+    TBK_CUDA(cudaMemsetAsync(p, 0, ba.bytes, st));                         // b_N = 0
+    TBK_TRY(scale_any(prec, cnt, vk.p, c_of(n_terms - 1), x, st));          // b_{N-1}
+    KStore ks;
+    ks.addv = vk.p;
+    for (int32_t k = n_terms - 2; k >= 1; --k) {
+      ks.addc[0] = coef[2 * k];
+      ks.addc[1] = coef[2 * k + 1];
+      TBK_TRY(step_ks(Ht, Rc, prec, x, p, p, false, part.as<double>(), grid, n_tiles, st, ks, 3));
+      std::swap(x, p);                                                      // x = b_k, p = b_{k+1}
     }
-    for (int32_t k = 2; k < n_terms; ++k) {
-      // T_k = 2 H~ T_{k-1} - T_{k-2}, written over T_{k-2}
-      TBK_TRY(step_any(Ht, Rc, prec, v_cur, v_prev, v_prev, false, part.as<double>(), grid, n_tiles, st));
-      std::swap(v_prev, v_cur);
-      TBK_TRY(axpy_any(prec, cnt, v_cur, c_of(k), acc.as<double2>(), false, st));
+    if (n_terms >= 2) {
+      // b_0 out of place (b_2 stays for the final combination)
+      ks.addc[0] = coef[0];
+      ks.addc[1] = coef[1];
+      TBK_TRY(step_ks(Ht, Rc, prec, x, bc.p, p, false, part.as<double>(), grid, n_tiles, st, ks, 3));
+      TBK_TRY(final_any(prec, cnt, bc.p, p, vk.p, c_of(0), acc.as<double2>(), st));
+    } else {
+      // one term: out = c_0 v  (= (b_0 - b_2 + c_0 v)/2 with b_0 = c_0 v, b_2 = 0)
+      TBK_TRY(final_any(prec, cnt, x, p, vk.p, c_of(0), acc.as<double2>(), st));
     }
     dim3 g((unsigned)((n + 31) / 32), (unsigned)((Rc + 31) / 32)), b(32, 8);
     unload_block_kernel<<<g, b, 0, st>>>(n, R, r0, std::min(Rc, R - r0), Rc, acc.as<double2>(), dst.as<double2>());

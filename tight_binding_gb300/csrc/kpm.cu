@@ -260,7 +260,7 @@ int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const vo
 }
 
 int step_ks(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
-            int grid, int n_tiles, cudaStream_t st, const KStore& ks) {
+            int grid, int n_tiles, cudaStream_t st, const KStore& ks, int mode) {
   StepArgs a;
   a.n = A->rows;
   a.n_tiles = n_tiles;
@@ -280,7 +280,7 @@ int step_ks(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const voi
   a.gather = 1;
   a.pf_dist = 1;
   a.ks = ks;
-  a.kst = 2;
+  a.kst = mode;
   a.pipe = A->ell.max_width > 4;
   return step_dispatch(A, Rc, prec, first, a, grid, st);
 }

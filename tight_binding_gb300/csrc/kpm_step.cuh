@@ -19,8 +19,10 @@ constexpr int kStepWarps = kStepThreads / 32;
 //                            FIRST: part[1] += <x|H x> (= <v_0|v_1>)
 //   braket:                  part[0] += <b|v_{s+1}>;  FIRST also part[1] += <b|x>
 //   gather == 0: no product at all (the last doubling step only needs the dots).
-//   KST: also write complex64 K-tiled stores (Kubo blocks, KStore): 1 = the
-//   output into one store; 2 = per column group the output or V x for an
+//   KST: 3 = add c v to the output (a Clenshaw step of a Chebyshev expansion,
+//   ks.addc / ks.addv); otherwise also write complex64 K-tiled stores (Kubo
+//   blocks, KStore): 1 = the output into one store; 2 = per column group the
+//   output or V x for an
 //   operator V with H's ELL structure, formed from the same gathered x (the
 //   operator product of the previous block fused into the step), so that the
 //   two sides of a Kubo pair can run as one recursion of twice the width.  A
@@ -140,6 +142,16 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
       if constexpr (FIRST) { out.re[q] = acc.re[q]; out.im[q] = acc.im[q]; }
       else { out.re[q] = F(2) * acc.re[q] - prev.re[q]; out.im[q] = F(2) * acc.im[q] - prev.im[q]; }
     }
+    if constexpr (KST == 3) {
+      // Clenshaw step of a Chebyshev expansion: b_k = 2 H b_{k+1} - b_{k+2} + c_k v
+      const LaneV<F, VPL> vv = ld_ro<F, VPL>(static_cast<const CT*>(ks.addv) + me * VPL);
+      const F cr = F(ks.addc[0]), ci = F(ks.addc[1]);
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) {
+        out.re[q] = out.re[q] + (cr * vv.re[q] - ci * vv.im[q]);
+        out.im[q] = out.im[q] + (cr * vv.im[q] + ci * vv.re[q]);
+      }
+    }
     // moment partial sums (before the store, from registers only)
     if constexpr (BRAKET) {
       const LaneV<F, VPL> b = ld_ro<F, VPL>(bras + me * VPL);
@@ -240,7 +252,10 @@ inline int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
     constexpr int VPLR = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
     if (a.kst == 2 && a.ks.halves == 2 && (R / 2) % VPLR != 0)
       return fail(TBK_ERR_UNSUPPORTED, "column groups narrower than a lane's vectors");
-    if (a.kst == 2) { if (first) TBK_STEP(true, false, 2); else TBK_STEP(false, false, 2); }
+    if (a.kst == 3) {
+      if (first) return fail(TBK_ERR_UNSUPPORTED, "Clenshaw term on a first step");
+      TBK_STEP(false, false, 3);
+    } else if (a.kst == 2) { if (first) TBK_STEP(true, false, 2); else TBK_STEP(false, false, 2); }
     else { if (first) TBK_STEP(true, false, 1); else TBK_STEP(false, false, 1); }
   } else if (first) { if (braket) TBK_STEP(true, true, 0); else TBK_STEP(true, false, 0); }
   else { if (braket) TBK_STEP(false, true, 0); else TBK_STEP(false, false, 0); }

@@ -137,6 +137,8 @@ struct KStore {
   int32_t usev[2] = {0, 0};
   int32_t kM = 0;
   int32_t halves = 1;
+  const void* addv = nullptr;      // Clenshaw steps: output += (addc[0] + i addc[1]) addv
+  double addc[2] = {0.0, 0.0};
 };
 
 // kpm.cu — one fused recursion step with the one-pass kernel in a precision
@@ -157,7 +159,7 @@ const void* ell_diag(const EllDev& E, int prec);
 // one recursion step (not the first block's braket form) writing the K-tiled
 // stores described by ks (output or operator products per column group)
 int step_ks(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
-            int grid, int n_tiles, cudaStream_t st, const KStore& ks);
+            int grid, int n_tiles, cudaStream_t st, const KStore& ks, int mode = 2);
 // true when B's sliced ELL has A's slices, widths and columns (values may differ)
 int same_ell_structure(tbk_sparse_s* A, tbk_sparse_s* B, bool* same, cudaStream_t st);
 int load_block_any(int prec, int32_t n, int32_t R, int32_t r0, int32_t Rp, const double2* src, void* dst,
