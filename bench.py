@@ -625,9 +625,9 @@ def run_expand(args):
     """exp(-i H t) applied to R = 8 random-phase vectors on the benchmark
     honeycomb (--cells^2 cells, disorder seed 1) through tbk_cheb_expand, in
     --precision, host vectors in and out (end to end, wall clock).  Algorithmic
-    bytes per term: H~ once (ELL off-diagonal index + value, diagonal value),
-    the recursion's three vector streams and the complex128 accumulator
-    (read + write) plus the re-read of the new term."""
+    bytes per term (one Clenshaw step): H~ once (ELL off-diagonal index +
+    value, diagonal value) and four vector streams (b_{k+1} gathered, b_{k+2}
+    read, b_k written, the kets read for the c_k term)."""
     import tight_binding_gb300 as tb
 
     X = tb.PartialLattice(tb.Honeycomb().add_hopping("A", 1, T_HOP), (args.cells, args.cells))
@@ -645,7 +645,7 @@ def run_expand(args):
     csz = {"mixed": 8, "fp64": 16, "dd": 16}[args.precision]      # complex element: c64, c128, 2 x (hi, lo) float
     vsz = {"mixed": 4, "fp64": 8, "dd": 8}[args.precision]        # real matrix value
     nnz_off = 3 * n
-    per_term = nnz_off * (4 + vsz) + n * vsz + n * R * (3 * csz + csz + 32)
+    per_term = nnz_off * (4 + vsz) + n * vsz + n * R * 4 * csz
     print(json.dumps({"expand": "exp(-iHt)", "t": args.expand, "terms": len(coef), "sites": n, "R": R,
                       "precision": args.precision, "s_e2e": dt,
                       "updates_per_s": n * R * len(coef) / dt, "GBps_e2e": per_term * len(coef) / dt / 1e9,
