@@ -198,6 +198,14 @@ int tbk_spectral_range(tbk_sparse A, int32_t iters, uint64_t seed, double* e_min
  * accumulated in complex128. */
 int tbk_cheb_expand(tbk_sparse Ht, int32_t n_terms, const double* coef, int32_t R, const double* kets, double* out,
                     int32_t precision, void* stream);
+/* Cheb_first_kind_seq_view(x, v), TB/numerical.h:346-361: next() yields
+ * (i, T_i(H~) v) for i = 0, 1, 2, ... (R column-major complex128 vectors, host
+ * in and out; block may be NULL to skip the copy); the two newest blocks stay
+ * on the device, one recursion step per call. */
+typedef struct tbk_cheb_view_s* tbk_cheb_view;
+int tbk_cheb_view_create(tbk_cheb_view* view, tbk_sparse Ht, int32_t R, const double* kets, int32_t precision);
+int tbk_cheb_view_next(tbk_cheb_view view, int32_t* index, double* block, void* stream);
+void tbk_cheb_view_destroy(tbk_cheb_view view);
 /* Delta-projection coefficients of conductivity_test_sawtooth (TB/snippets.h:
  * 175, 194-202): coef_k = a_d(k) T_k(e), a_d(0) = 1, a_d(k>0) = 2, for
  * k = 0 .. N (N + 1 complex values). */

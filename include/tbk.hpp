@@ -6,6 +6,7 @@
 //   GreenFunction / GreenFunctionImag  TB/lattice.h:545-647
 //   matrix_spectral_range_sparse       TB/numerical.h:24-46 (device Lanczos)
 //   cheb_expand / time_evolve          TB/numerical.h:346-361
+//   Cheb_first_kind_seq_view           TB/numerical.h:346-361
 //   cuda::Cheb_first_kind_seq_braket   TB/numerics_cuda.cuh:10-13
 //   bases_of_uniform_ampl_with_random_phases  TB/numerical.h:120-122 (seeded)
 //   density_of_states_seq              TB/functions.h:15-32
@@ -330,6 +331,29 @@ inline MatrixXcd cheb_expand(const SparseMatrix& Ht, const std::vector<Complex>&
                         kets.raw(), out.raw(), precision, nullptr));
   return out;
 }
+// numerical::Chebyshev::Cheb_first_kind_seq_view (TB/numerical.h:346-361):
+// next() -> {i, T_i(x) v}; the recursion state stays on the device
+class Cheb_first_kind_seq_view {
+ public:
+  Cheb_first_kind_seq_view(const SparseMatrix& x, const MatrixXcd& v, int precision = TBK_PREC_FP64)
+      : rows_(v.rows), cols_(v.cols) {
+    check(tbk_cheb_view_create(&h_, x.handle(), v.cols, v.raw(), precision));
+  }
+  Cheb_first_kind_seq_view(const Cheb_first_kind_seq_view&) = delete;
+  Cheb_first_kind_seq_view& operator=(const Cheb_first_kind_seq_view&) = delete;
+  ~Cheb_first_kind_seq_view() { tbk_cheb_view_destroy(h_); }
+  std::pair<int, MatrixXcd> next() {
+    MatrixXcd out(rows_, cols_);
+    int32_t i = 0;
+    check(tbk_cheb_view_next(h_, &i, out.raw(), nullptr));
+    return {i, out};
+  }
+
+ private:
+  tbk_cheb_view h_ = nullptr;
+  int32_t rows_, cols_;
+};
+
 // exp(-i HE t) kets for the Hamiltonian of G (HE = a scaled_HE + b)
 inline MatrixXcd time_evolve(const GreenFunction& G, double t, const MatrixXcd& kets, double tol = 1e-15,
                              int precision = TBK_PREC_FP64) {

@@ -206,3 +206,20 @@ def test_builder_random_vacancies_device_compaction(gpu):
     n_kept = X.get_kept_number()
     cp = H.to_csc()[0]
     assert n_kept == 2 * 256 * 192 - 4300 and cp[n_kept] == cp[-1]
+
+
+def test_builder_every_site_removed(gpu):
+    """remove_atoms_random of every cell on both sublattices: the open-BC
+    Hamiltonian keeps its total_number shape with no entries (the reference's
+    index_c is all -1), as the oracle builds it."""
+    tb = gpu
+    cell = tb.Honeycomb().add_hopping("A", 1, 1.0)
+    X = tb.PartialLattice(cell, (5, 4))
+    X.remove_atoms_random("A", 20, seed=1)
+    X.remove_atoms_random("B", 20, seed=2)
+    assert X.get_kept_number() == 0
+    H = X.get_Hamiltonian_sparse(float)
+    ref = orc.build_csc(spec_from(cell, (5, 4), mode=orc.MODE_SPARSE, is_complex=False,
+                                  removed=X.removed_sites().astype(np.int32)))
+    _assert_same(H, ref)
+    assert H.to_csc()[0][-1] == 0

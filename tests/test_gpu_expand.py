@@ -104,3 +104,26 @@ def test_conductivity_test_sawtooth_matches_oracle(gpu):
     kL = V @ orc.cheb_expand(n, cp, ri, v, coef, V @ kets)
     ref = np.sum(kL.real * kR.real + kL.imag * kR.imag) / R
     assert abs(got - ref) <= 1e-10 * max(1.0, abs(ref)), (got, ref)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "dd", "mixed"])
+def test_cheb_first_kind_seq_view(gpu, precision):
+    """Cheb_first_kind_seq_view (TB/numerical.h:346-361): next() yields
+    (i, T_i(H~) v) in order, against the oracle's blocks; more vectors than one
+    chunk; Cheb_first_kind_seq_on_bases collects the same blocks."""
+    tb = gpu
+    G = _honeycomb(tb, (7, 6))
+    Ht = G.scaled_HE
+    n = Ht.shape[0]
+    kets = tb.bases_of_uniform_ampl_with_random_phases(n, 40, 3)
+    cp, ri, v = Ht.to_csc()
+    ref = orc.cheb_blocks(n, cp, ri, v, 9, kets)                 # (K, R, n)
+    view = tb.Cheb_first_kind_seq_view(Ht, kets, precision)
+    tol = {"fp64": 1e-13, "dd": 1e-13, "mixed": 1e-5}[precision]
+    for k in range(9):
+        i, blk = view.next()
+        assert i == k
+        assert np.max(np.abs(blk - ref[k].T)) <= tol * max(1.0, np.max(np.abs(ref[k])))
+    blocks = tb.Cheb_first_kind_seq_on_bases(Ht, 4, kets[:, 0], precision)
+    for k in range(4):
+        assert np.max(np.abs(blocks[k] - ref[k][0])) <= tol * max(1.0, np.max(np.abs(ref[k])))

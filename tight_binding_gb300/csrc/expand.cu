@@ -115,6 +115,17 @@ int final_any(int prec, int64_t cnt, const void* b0, const void* b2, const void*
 
 using namespace tbk;
 
+// Cheb_first_kind_seq_view (TB/numerical.h:346-361): the two newest blocks of
+// each chunk of vectors stay on the device; next() hands out T_i v and
+// advances one recursion step.
+struct tbk_cheb_view_s {
+  tbk_sparse_s* H = nullptr;
+  int32_t n = 0, R = 0, Rc = 0, n_chunks = 0, prec = 0, i = 0;
+  int grid = 1, n_tiles = 1;
+  std::vector<DevBuf> cur, nxt;      // per chunk: T_i v, T_{i+1} v (site-major)
+  DevBuf acc, dst, part;
+};
+
 extern "C" {
 
 int tbk_cheb_expand(tbk_sparse Ht, int32_t n_terms, const double* coef, int32_t R, const double* kets, double* out,
@@ -175,6 +186,82 @@ int tbk_cheb_expand(tbk_sparse Ht, int32_t n_terms, const double* coef, int32_t 
   TBK_CUDA(cudaMemcpyAsync(out, dst.p, sizeof(double2) * (size_t)n * R, cudaMemcpyDeviceToHost, st));
   TBK_CUDA(cudaStreamSynchronize(st));
   return TBK_OK;
+}
+
+int tbk_cheb_view_create(tbk_cheb_view* out, tbk_sparse Ht, int32_t R, const double* kets, int32_t precision) {
+  if (!out || !Ht || !kets || R < 1) return fail(TBK_ERR_INVALID, "tbk_cheb_view_create: bad argument");
+  *out = nullptr;
+  if (Ht->rows != Ht->cols) return fail(TBK_ERR_INVALID, "tbk_cheb_view_create: matrix must be square");
+  if (precision != TBK_PREC_FP64 && precision != TBK_PREC_MIXED && precision != TBK_PREC_DD)
+    return fail(TBK_ERR_INVALID, "tbk_cheb_view_create: unknown precision %d", precision);
+  cudaStream_t st = nullptr;
+  auto* V = new tbk_cheb_view_s();
+  V->H = Ht;
+  V->n = Ht->rows;
+  V->R = R;
+  V->prec = precision;
+  V->Rc = chunk_width(precision, R);
+  V->n_chunks = (R + V->Rc - 1) / V->Rc;
+  auto bail = [&](int rc) { delete V; return rc; };
+  int rc = step_config(Ht, V->Rc, precision, &V->grid, &V->n_tiles, st);
+  if (rc != TBK_OK) return bail(rc);
+  const int64_t cnt = (int64_t)Ht->ell.n_slices * 32 * V->Rc;
+  const size_t csz = precision == TBK_PREC_MIXED ? sizeof(float2) : precision == TBK_PREC_DD ? sizeof(dd2) : sizeof(double2);
+  V->cur.resize(V->n_chunks);
+  V->nxt.resize(V->n_chunks);
+  DevBuf src;
+  if ((rc = src.alloc(sizeof(double2) * (size_t)V->n * R)) != TBK_OK || (rc = V->acc.alloc(sizeof(double2) * cnt)) != TBK_OK ||
+      (rc = V->dst.alloc(sizeof(double2) * (size_t)V->n * R)) != TBK_OK ||
+      (rc = V->part.alloc(sizeof(double) * 2 * V->grid)) != TBK_OK)
+    return bail(rc);
+  if (cudaMemcpy(src.p, kets, sizeof(double2) * (size_t)V->n * R, cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(TBK_ERR_CUDA, "tbk_cheb_view_create: upload failed"));
+  for (int32_t c = 0; c < V->n_chunks; ++c) {
+    if ((rc = V->cur[c].alloc(csz * cnt)) != TBK_OK || (rc = V->nxt[c].alloc(csz * cnt)) != TBK_OK) return bail(rc);
+    cudaMemsetAsync(V->cur[c].p, 0, V->cur[c].bytes, st);
+    cudaMemsetAsync(V->nxt[c].p, 0, V->nxt[c].bytes, st);
+    // v_0 = v, v_1 = x v (the view's constructor)
+    if ((rc = load_block_any(precision, V->n, R, c * V->Rc, V->Rc, src.as<double2>(), V->cur[c].p, st)) != TBK_OK ||
+        (rc = step_any(Ht, V->Rc, precision, V->cur[c].p, V->nxt[c].p, nullptr, true, V->part.as<double>(), V->grid,
+                       V->n_tiles, st)) != TBK_OK)
+      return bail(rc);
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess) return bail(fail(TBK_ERR_CUDA, "tbk_cheb_view_create: sync failed"));
+  *out = V;
+  return TBK_OK;
+}
+
+int tbk_cheb_view_next(tbk_cheb_view V, int32_t* index, double* block, void* stream) {
+  if (!V) return fail(TBK_ERR_INVALID, "tbk_cheb_view_next: null view");
+  cudaStream_t st = as_stream(stream);
+  const int64_t cnt = (int64_t)V->H->ell.n_slices * 32 * V->Rc;
+  for (int32_t c = 0; c < V->n_chunks; ++c) {
+    if (block) {
+      // T_i v of this chunk -> complex128 -> columns of the host block
+      TBK_TRY(final_any(V->prec, cnt, V->cur[c].p, V->cur[c].p, V->cur[c].p, make_double2(2.0, 0.0),
+                        V->acc.as<double2>(), st));                    // (a - a + 2 a) / 2 = a, exactly
+      dim3 g((unsigned)((V->n + 31) / 32), (unsigned)((V->Rc + 31) / 32)), b(32, 8);
+      unload_block_kernel<<<g, b, 0, st>>>(V->n, V->R, c * V->Rc, std::min(V->Rc, V->R - c * V->Rc), V->Rc,
+                                           V->acc.as<double2>(), V->dst.as<double2>());
+      TBK_CHECK_LAUNCH();
+    }
+    // T_{i+2} = 2 x T_{i+1} - T_i, written over T_i; then cur <-> nxt
+    TBK_TRY(step_any(V->H, V->Rc, V->prec, V->nxt[c].p, V->cur[c].p, V->cur[c].p, false, V->part.as<double>(),
+                     V->grid, V->n_tiles, st));
+    std::swap(V->cur[c], V->nxt[c]);
+  }
+  if (block)
+    TBK_CUDA(cudaMemcpyAsync(block, V->dst.p, sizeof(double2) * (size_t)V->n * V->R, cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  if (index) *index = V->i;
+  ++V->i;
+  return TBK_OK;
+}
+
+void tbk_cheb_view_destroy(tbk_cheb_view V) {
+  if (!V) return;
+  cudaDeviceSynchronize();
+  delete V;
 }
 
 int tbk_cheb_coef_delta(double e, int32_t N, double* coef) {

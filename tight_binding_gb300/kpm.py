@@ -269,6 +269,45 @@ def cheb_expand(Ht: SparseMatrix, coef, kets, precision="dd") -> np.ndarray:
     return out.reshape(kets.shape) if kets.ndim == 1 else out
 
 
+class Cheb_first_kind_seq_view:
+    """Cheb_first_kind_seq_view(x, v), TB/numerical.h:346-361: next() returns
+    (i, T_i(x) v) for i = 0, 1, 2, ...; the recursion state stays on the device
+    (one step per call, the block copied to the host)."""
+
+    def __init__(self, x: SparseMatrix, v, precision="fp64"):
+        v = np.asarray(v)
+        self._vec = v.ndim == 1
+        self._K = _block(v, x.shape[0])
+        h = C.c_void_p()
+        check(lib().tbk_cheb_view_create(C.byref(h), x.handle, self._K.shape[1], capi.ptr(self._K), _prec(precision)))
+        self._h = h
+
+    def next(self):
+        out = np.zeros(self._K.shape, dtype=np.complex128, order="F")
+        i = C.c_int32()
+        check(lib().tbk_cheb_view_next(self._h, C.byref(i), capi.ptr(out), None))
+        return i.value, (out[:, 0] if self._vec else out)
+
+    def __iter__(self):
+        while True:
+            yield self.next()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().tbk_cheb_view_destroy(h)
+            except Exception:
+                pass
+            self._h = C.c_void_p()
+
+
+def Cheb_first_kind_seq_on_bases(x: SparseMatrix, n: int, v, precision="fp64") -> list:
+    """TB/numerical.h:333-344: [T_0(x) v, ..., T_{n-1}(x) v] (all blocks on the host)."""
+    view = Cheb_first_kind_seq_view(x, v, precision)
+    return [view.next()[1] for _ in range(n)]
+
+
 def sparse_apply(A: SparseMatrix, kets, precision="dd") -> np.ndarray:
     """A @ kets on the device (T_1(A) kets)."""
     return cheb_expand(A, [0.0, 1.0], kets, precision)
