@@ -17,6 +17,7 @@
 //   8. remove_atoms_random on a honeycomb: the open-BC Hamiltonian keeps
 //      total - n columns with entries, the rest empty (compressed index)
 //   9. moment file round trip through tbk_moments_save / tbk_moments_load
+//  10. Cheb_first_kind_seq_view on a ring plane wave: T_i(H~) v = T_i(lambda) v
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -222,6 +223,28 @@ int main() {
     std::remove(path);
     const bool ok = back == mu && g.R == 8 && g.seed == 42 && std::string(g.label) == "square 64x64";
     expect(ok, "moment file round trip", 0.0);
+  }
+  // ---- 10. Cheb_first_kind_seq_view
+  {
+    const int L = 64;
+    UnitCell<1> chain({{1, 0, 0}}, {{"A", {0, 0, 0}}});
+    chain.add_hopping("A", 1, Complex(1.0, 0.0));
+    PartialLattice<1> X(chain, {L});
+    SparseMatrix H = X.get_Hamiltonian_periodic_extend_bare_sparse<double>({1});
+    GreenFunction G(16, H, -2.1, 2.1);
+    const double kq = 2 * pi * 5 / L, lam = 2.0 * std::cos(kq) / 2.1;
+    MatrixXcd psi(L, 1);
+    for (int i = 0; i < L; ++i) psi(i, 0) = std::polar(1.0 / std::sqrt((double)L), kq * i);
+    Cheb_first_kind_seq_view view(G.scaled_HE, psi);
+    double err = 0.0;
+    bool order = true;
+    for (int k = 0; k < 6; ++k) {
+      auto [i, blk] = view.next();
+      order = order && i == k;
+      const double t = std::cos(k * std::acos(lam));
+      for (int r = 0; r < L; ++r) err = std::fmax(err, std::abs(blk(r, 0) - t * psi(r, 0)));
+    }
+    expect(order && err <= 1e-13, "Cheb_first_kind_seq_view on a plane wave", err);
   }
   std::printf("%s\n", failures ? "FAILED" : "ALL PASSED");
   return failures ? 1 : 0;
