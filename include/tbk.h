@@ -299,6 +299,10 @@ int tbk_random_phase_kets(int32_t n, int32_t R, uint64_t seed, double* kets);
  * ========================================================================= */
 enum { TBK_KERNEL_DIRICHLET = 0, TBK_KERNEL_FEJER = 1, TBK_KERNEL_LORENTZ = 2,
        TBK_KERNEL_JACKSON = 3, TBK_KERNEL_LANCZOS = 4, TBK_KERNEL_WANG_ZUNGER = 5 };
+/* expn_coef_alpha_seq(z, n), TB/numerical.h:304-316: the Chebyshev
+ * coefficients of the resolvent, 1/(z - x) = sum_k alpha_k(z) T_k(x), n complex
+ * values (interleaved re/im, host math). */
+int tbk_expn_coef_alpha_seq(double z_re, double z_im, int32_t n, double* alpha);
 /* kernel_seq(N, kernel), TB/numerical.h:393-447.  p0/p1: lambda (Lorentz),
  * M (Lanczos), alpha/beta (Wang-Zunger).  g_out: N doubles, host. */
 int tbk_kernel_seq(int32_t kind, int32_t N, double p0, double p1, double* g_out);

@@ -331,6 +331,14 @@ inline MatrixXcd cheb_expand(const SparseMatrix& Ht, const std::vector<Complex>&
                         kets.raw(), out.raw(), precision, nullptr));
   return out;
 }
+// numerical::Chebyshev::expn_coef_alpha_seq (TB/numerical.h:304-316):
+// 1/(z - x) = sum_k alpha_k(z) T_k(x)
+inline std::vector<Complex> expn_coef_alpha_seq(Complex z, int n) {
+  std::vector<Complex> a((size_t)n);
+  check(tbk_expn_coef_alpha_seq(z.real(), z.imag(), n, reinterpret_cast<double*>(a.data())));
+  return a;
+}
+
 // numerical::Chebyshev::Cheb_first_kind_seq_view (TB/numerical.h:346-361):
 // next() -> {i, T_i(x) v}; the recursion state stays on the device
 class Cheb_first_kind_seq_view {

@@ -216,6 +216,13 @@ def kernel_seq(kind, N, p0=0.0, p1=0.0):
     return g
 
 
+def expn_coef_alpha_seq(z, n):
+    out = np.zeros(2 * n)
+    z = complex(z)
+    lib().tbo_expn_coef_alpha_seq(z.real, z.imag, n, _p(out))
+    return out.view(np.complex128)
+
+
 def green_imag_eval(g, mu, z):
     g = np.ascontiguousarray(g, dtype=np.float64)
     mu = np.ascontiguousarray(mu, dtype=np.float64)

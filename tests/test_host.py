@@ -161,3 +161,16 @@ def test_new_entry_points_reject_bad_arguments_without_gpu(tb):
     k = C.c_int32()
     assert L.tbk_cheb_evolution_terms(1.0, 1.0, 0.0, C.byref(k)) == capi.TBK_ERR_INVALID
     assert L.tbk_moments_save(None, None, None) == capi.TBK_ERR_INVALID
+
+
+def test_expn_coef_alpha_seq_host(tb):
+    """expn_coef_alpha_seq (TB/numerical.h:304-316) against the oracle's, and
+    the resolvent identity 1/(z - x) = sum_k alpha_k(z) T_k(x) off the cut."""
+    import oracle as orc
+    for z in (0.3 + 0.01j, -0.9 + 1e-3j, 1.7 - 0.2j, 0.0 + 0.5j):
+        a = tb.expn_coef_alpha_seq(z, 64)
+        assert np.allclose(a, orc.expn_coef_alpha_seq(z, 64), rtol=1e-13, atol=1e-15)
+    z, x = 0.2 + 0.4j, 0.35
+    a = tb.expn_coef_alpha_seq(z, 400)
+    T = np.cos(np.arange(400) * np.arccos(x))
+    assert abs(np.sum(a * T) - 1.0 / (z - x)) <= 1e-10

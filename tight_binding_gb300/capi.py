@@ -116,6 +116,7 @@ SIGNATURES = {
     "tbk_moments_save": (C.c_int, [_cp, _vp, _vp]),
     "tbk_moments_load_header": (C.c_int, [_cp, _vp]),
     "tbk_moments_load": (C.c_int, [_cp, _vp, _vp, _i64]),
+    "tbk_expn_coef_alpha_seq": (C.c_int, [C.c_double, C.c_double, _i32, _vp]),
     "tbk_cheb_view_create": (C.c_int, [C.POINTER(_vp), _vp, _i32, _vp, _i32]),
     "tbk_cheb_view_next": (C.c_int, [_vp, _pi32, _vp, _vp]),
     "tbk_cheb_view_destroy": (None, [_vp]),

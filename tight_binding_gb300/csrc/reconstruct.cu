@@ -8,6 +8,7 @@
 //   density_of_states_seq     TB/functions.h:26-30
 #include <cuda_runtime.h>
 
+#include <complex>
 #include <vector>
 
 #include "tbk_internal.h"
@@ -105,6 +106,25 @@ static int upload(DevBuf& b, const T* h, size_t n, cudaStream_t st) {
 using namespace tbk;
 
 extern "C" {
+
+int tbk_expn_coef_alpha_seq(double z_re, double z_im, int32_t n, double* alpha) {
+  if (n < 1 || !alpha) return fail(TBK_ERR_INVALID, "tbk_expn_coef_alpha_seq: bad argument");
+  // 1/(z - x) = sum_k alpha_k(z) T_k(x), TB/numerical.h:304-316: s1 = sqrt(1 - z^2)
+  // (principal branch), alpha_0 = -i / s1, alpha_k = -2i (z - i s1)^k / s1
+  const std::complex<double> z(z_re, z_im), I(0.0, 1.0);
+  const std::complex<double> s1 = std::sqrt(1.0 - z * z);
+  const std::complex<double> s2 = z - I * s1;
+  std::complex<double> sn = -2.0 * I / s1;
+  const std::complex<double> a0 = -I / s1;
+  alpha[0] = a0.real();
+  alpha[1] = a0.imag();
+  for (int32_t k = 1; k < n; ++k) {
+    sn *= s2;
+    alpha[2 * k] = sn.real();
+    alpha[2 * k + 1] = sn.imag();
+  }
+  return TBK_OK;
+}
 
 int tbk_kernel_seq(int32_t kind, int32_t N, double p0, double p1, double* g_out) {
   if (N < 1 || !g_out) return fail(TBK_ERR_INVALID, "tbk_kernel_seq: bad argument");

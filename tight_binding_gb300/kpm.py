@@ -154,6 +154,14 @@ def Wang_and_Zunger(alpha: float, beta: float) -> Kernel:
     return Kernel(capi.KERNEL_WANG_ZUNGER, alpha, beta)
 
 
+def expn_coef_alpha_seq(z: complex, n: int) -> np.ndarray:
+    """TB/numerical.h:304-316: alpha_k(z) with 1/(z - x) = sum_k alpha_k(z) T_k(x)."""
+    a = np.zeros(n, dtype=np.complex128)
+    z = complex(z)
+    check(lib().tbk_expn_coef_alpha_seq(z.real, z.imag, int(n), capi.ptr(a)))
+    return a
+
+
 def kernel_seq(N: int, kernel: Kernel) -> np.ndarray:
     return kernel.seq(N)
 
