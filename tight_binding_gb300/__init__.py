@@ -12,7 +12,8 @@ from .kubo import (bastin_integrate, bastin_zeta, chebyshev_nodes, conductivity_
                    conductivity_test_sawtooth)
 from .kpm import (Cheb_first_kind_seq_braket, Dirichlet, Fejer, GreenFunction, GreenFunctionImag, Jackson,
                   KpmSolver, Kernel, Lanczos, Lorentz, Wang_and_Zunger, bases_of_uniform_ampl_with_random_phases,
-                  density_of_states_function, density_of_states_seq, dos_from_moments, kernel_seq, expn_coef_alpha_seq,
+                  density_of_states_function, density_of_states_seq, dos_from_moments, kernel_seq, expn_coef_alpha_seq, trace_braket,
+                  trace_braket_complex,
                   spectral_range, cheb_expand, sparse_apply, Cheb_first_kind_seq_view,
                   Cheb_first_kind_seq_on_bases, delta_coefficients, evolution_coefficients,
                   evolution_terms, time_evolve)

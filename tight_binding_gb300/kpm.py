@@ -154,6 +154,18 @@ def Wang_and_Zunger(alpha: float, beta: float) -> Kernel:
     return Kernel(capi.KERNEL_WANG_ZUNGER, alpha, beta)
 
 
+def trace_braket(bras_T, kets) -> float:
+    """TB/numerical.h:126-135: sum_ij Re b_ij Re k_ij + Im b_ij Im k_ij (host)."""
+    b = np.asarray(bras_T)
+    k = np.asarray(kets)
+    return float(np.sum(b.real * k.real + b.imag * k.imag))
+
+
+def trace_braket_complex(bras_T, kets) -> complex:
+    """TB/numerical.h:136-144: sum_ij conj(b_ij) k_ij (host)."""
+    return complex(np.sum(np.conj(np.asarray(bras_T)) * np.asarray(kets)))
+
+
 def expn_coef_alpha_seq(z: complex, n: int) -> np.ndarray:
     """TB/numerical.h:304-316: alpha_k(z) with 1/(z - x) = sum_k alpha_k(z) T_k(x)."""
     a = np.zeros(n, dtype=np.complex128)
