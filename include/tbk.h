@@ -417,10 +417,24 @@ typedef struct {
   int32_t is_complex;                /* Scalar of H (0: double, 1: complex)       */
   int32_t n_mom;                     /* M >= 2                                    */
   int32_t R;                         /* random-phase vectors >= 1                 */
-  int32_t precision;                 /* TBK_PREC_MIXED or TBK_PREC_FP64           */
+  int32_t precision;                 /* TBK_PREC_MIXED, TBK_PREC_FP64 or _DD      */
   uint64_t seed;
   double e_min, e_max;               /* spectral bounds of H (e_max > e_min)      */
+  /* conductivity requests (zero for the DoS moments): */
+  int32_t kind;                      /* TBK_REQ_*                                 */
+  int32_t axis[2];                   /* position axes a, b of v_a = [x_a, H~]     */
+  int32_t kernel;                    /* TBK_KERNEL_* applied to mu_nm             */
+  double kernel_p0, kernel_p1;       /* its parameters (Lorentz: lambda)          */
 } tbk_request;
+/* Request kinds.  DOS: mu_n, n < n_mom (doubling recursion), the moments of
+ * density_of_states.  KUBO_BASTIN: g_m g_n mu_nm with mu_nm = <T_m r | v_a T_n v_b r>
+ * summed over the R vectors (conductivity_Kubo_Bastin, TB/snippets.h:306-456);
+ * KUBO_GREENWOOD: mu_nm = <v_a T_m v_a r | T_n r> (conductivity_spectrum,
+ * TB/snippets.h:225-304).  Kubo results are n_mom x n_mom complex128 (row
+ * major, 2 n_mom^2 doubles); they run as one tbk_kubo_mu solve on the
+ * admission stream while the DoS rounds continue on theirs, with the stored
+ * blocks charged to the HBM budget. */
+enum { TBK_REQ_DOS = 0, TBK_REQ_KUBO_BASTIN = 1, TBK_REQ_KUBO_GREENWOOD = 2 };
 int tbk_server_create(tbk_server* out, const tbk_server_config* cfg);
 /* Stops admitting, lets the rounds in flight end, fails what is still queued
  * or resident, frees everything. */
@@ -429,7 +443,7 @@ void tbk_server_destroy(tbk_server server);
  * alone exceeds the budget. */
 int tbk_server_submit(tbk_server server, const tbk_request* req, int64_t* ticket);
 /* Waits up to wait_ms (>= 0) for the request.  Done: copies the n_mom moments
- * to mu_out, times_ms[4] = {queued, build, resident, total} (may be NULL),
+ * (Kubo requests: the 2 n_mom^2 doubles of mu_nm) to mu_out, times_ms[4] = {queued, build, resident, total} (may be NULL),
  * forgets the ticket and returns TBK_OK.  Not done: TBK_PENDING.  Failed: its
  * status (and forgets the ticket). */
 int tbk_server_poll(tbk_server server, int64_t ticket, int32_t wait_ms, double* mu_out,

@@ -422,6 +422,34 @@ class DosServer {
     n_mom_[t] = n_mom;
     return t;
   }
+  // conductivity request (TBK_REQ_KUBO_BASTIN / _GREENWOOD): H of X with the
+  // given periodic axes (complex), v_a = [x_a, H~]; poll returns the
+  // 2 M^2 doubles of g_m g_n mu_nm (row-major complex)
+  template <int Dim>
+  int64_t submit_kubo(const PartialLattice<Dim>& X, int kind, int M, int R, uint64_t seed, double e_min,
+                      double e_max, std::array<int, 2> axes, LatticeVector<Dim> periodic, int kernel = TBK_KERNEL_LORENTZ,
+                      double kernel_p0 = 6.0, int precision = TBK_PREC_DD) {
+    tbk_request q{};
+    q.lattice = X.handle();
+    q.build_mode = TBK_BUILD_PERIODIC_BARE;
+    for (int i = 0; i < 3; ++i) q.extend[i] = i < Dim ? periodic[i] : 0;
+    q.is_complex = 1;
+    q.n_mom = M;
+    q.R = R;
+    q.precision = precision;
+    q.seed = seed;
+    q.e_min = e_min;
+    q.e_max = e_max;
+    q.kind = kind;
+    q.axis[0] = axes[0];
+    q.axis[1] = axes[1];
+    q.kernel = kernel;
+    q.kernel_p0 = kernel_p0;
+    int64_t t = 0;
+    check(tbk_server_submit(h_, &q, &t));
+    n_mom_[t] = 2 * M * M;
+    return t;
+  }
   // true and the moments when done within wait_ms; throws if the request failed
   bool poll(int64_t ticket, int wait_ms, std::vector<double>& mu, double times_ms[4] = nullptr) {
     mu.resize((size_t)n_mom_.at(ticket));

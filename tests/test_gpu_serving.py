@@ -182,3 +182,61 @@ def test_failed_build_fails_only_its_request(gpu):
         st = srv.stats()
     assert st["done"] == 2 and st["failed"] == 1 and st["reserved_bytes"] == 0
     assert np.all(np.isfinite(r1)) and np.all(np.isfinite(r3)) and not np.array_equal(r1, r3)
+
+
+def _kubo_lattice(tb):
+    X = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (24, 20))
+    G = np.zeros((3, 3))
+    G[1, 0] = 2 * np.pi / 32
+    X.set_gauge_linear(G, np.zeros(3))
+    X.set_scalar_disorder(0.5, 3)
+    return X
+
+
+@pytest.mark.parametrize("kind", ["bastin", "greenwood"])
+def test_kubo_requests_equal_direct_solve(gpu, kind):
+    """A conductivity request through the server gives the bits of the direct
+    tbk_kubo_mu solve on the same H~, commutators, seed and kernel, also while
+    DoS requests run beside it; the DoS results keep their alone bits."""
+    tb = gpu
+    X = _kubo_lattice(tb)
+    M, R, seed, lo, hi = 48, 4, 7, -4.4, 4.4
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([0, 1], complex)
+    Gf = tb.GreenFunction(M, H, lo, hi)
+    vx = tb.commutator(Gf.scaled_HE, X.op_position(0))
+    vy = tb.commutator(Gf.scaled_HE, X.op_position(1))
+    kw = dict(M=M, R=R, seed=seed, kernel=tb.Lorentz(6.0), tensor=True, recursion="dd")
+    if kind == "bastin":
+        direct = tb.kubo_mu(Gf.scaled_HE, None, None, vx, vy, **kw)
+    else:
+        direct = tb.kubo_mu(Gf.scaled_HE, vx, vx, None, None, **kw)
+    dos_cases = CASES[:4]
+    with tb.DosServer(autotune=False, steps_per_round=8) as srv:
+        alone = []
+        for i, (k, L, W, Mm, Rr, prec) in enumerate(dos_cases):
+            Xd = lattice(tb, k, L, W, seed=200 + i)
+            alone.append(srv.result(srv.submit(Xd, Mm, Rr, seed=i, e_min=bounds(k, W)[0], e_max=bounds(k, W)[1],
+                                               precision=prec))[0])
+        tickets = []
+        for i, (k, L, W, Mm, Rr, prec) in enumerate(dos_cases[:2]):
+            Xd = lattice(tb, k, L, W, seed=200 + i)
+            tickets.append(srv.submit(Xd, Mm, Rr, seed=i, e_min=bounds(k, W)[0], e_max=bounds(k, W)[1], precision=prec))
+        tk = srv.submit_kubo(X, kind, M, R, seed, lo, hi, axes=(0, 1), kernel=tb.Lorentz(6.0), precision="dd",
+                             extend=[0, 1], scalar=complex)
+        for i, (k, L, W, Mm, Rr, prec) in enumerate(dos_cases[2:]):
+            Xd = lattice(tb, k, L, W, seed=202 + i)
+            tickets.append(srv.submit(Xd, Mm, Rr, seed=2 + i, e_min=bounds(k, W)[0], e_max=bounds(k, W)[1],
+                                      precision=prec))
+        mu, times = srv.result(tk, timeout_s=300)
+        assert mu.shape == (M, M) and np.array_equal(mu, direct)
+        for i, t in enumerate(tickets):
+            assert np.array_equal(srv.result(t, timeout_s=300)[0], alone[i])
+        assert srv.stats()["failed"] == 0
+
+
+def test_kubo_request_over_budget_is_refused(gpu):
+    tb = gpu
+    X = tb.PartialLattice(tb.FCC().add_hopping("A", 1, 1.0), (64, 64, 64))
+    with tb.DosServer(budget_gb=2.0, autotune=False) as srv:
+        with pytest.raises(tb.TbkError, match="budget"):
+            srv.submit_kubo(X, "greenwood", 1024, 8, 0, -13.0, 13.0, axes=(0,), extend=[1, 1, 1], scalar=float)

@@ -70,7 +70,12 @@ class Request(C.Structure):
     """tbk_request"""
     _fields_ = [("lattice", C.c_void_p), ("build_mode", C.c_int32), ("extend", C.c_int32 * 3),
                 ("is_complex", C.c_int32), ("n_mom", C.c_int32), ("R", C.c_int32), ("precision", C.c_int32),
-                ("seed", C.c_uint64), ("e_min", C.c_double), ("e_max", C.c_double)]
+                ("seed", C.c_uint64), ("e_min", C.c_double), ("e_max", C.c_double),
+                ("kind", C.c_int32), ("axis", C.c_int32 * 2), ("kernel", C.c_int32),
+                ("kernel_p0", C.c_double), ("kernel_p1", C.c_double)]
+
+
+REQ_DOS, REQ_KUBO_BASTIN, REQ_KUBO_GREENWOOD = 0, 1, 2
 
 
 _pcfg, _preq = C.POINTER(ServerConfig), C.POINTER(Request)

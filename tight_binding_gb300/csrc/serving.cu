@@ -361,6 +361,13 @@ struct Footprint {
 
 int check_request(const tbk_request* q) {
   if (!q || !q->lattice) return fail(TBK_ERR_INVALID, "request: null argument");
+  if (q->kind < TBK_REQ_DOS || q->kind > TBK_REQ_KUBO_GREENWOOD) return fail(TBK_ERR_INVALID, "unknown request kind %d", q->kind);
+  if (q->kind != TBK_REQ_DOS) {
+    const int dim = q->lattice->cell.dim;
+    for (int k = 0; k < 2; ++k)
+      if (q->axis[k] < 0 || q->axis[k] >= dim) return fail(TBK_ERR_INVALID, "Error: axis out of range.");
+    if (q->kernel < 0 || q->kernel > 5) return fail(TBK_ERR_INVALID, "unknown kernel %d", q->kernel);
+  }
   if (q->n_mom < 2) return fail(TBK_ERR_INVALID, "n must be greater than or equal to 2");
   if (q->R < 1) return fail(TBK_ERR_INVALID, "R must be >= 1");
   if (q->precision != TBK_PREC_MIXED && q->precision != TBK_PREC_FP64 && q->precision != TBK_PREC_DD)
@@ -375,6 +382,41 @@ int check_request(const tbk_request* q) {
 // Bytes the request holds at each phase of its build and once resident.  Entry
 // bounds: a site of atom a has at most deg(a) = #hopping terms touching a
 // off-diagonal entries, plus the diagonal.
+static_assert(sizeof(tbk_request) == 96, "tbk_request layout is part of the C ABI");
+
+int kubo_chunk(int R) {
+  int c = 1;
+  while (c < R && c < 32) c <<= 1;
+  return c;
+}
+
+Footprint footprint_of(const tbk_request& q, const tbk_lattice_s& L);
+
+// Conductivity request: matrices (H, H~, two position diagonals, two
+// commutators, their ELLs), both stored block sides at the chunk width that
+// fits the budget, the work blocks and the mu_nm accumulators.
+Footprint kubo_footprint(const tbk_request& q, const tbk_lattice_s& L, double budget, int* chunk) {
+  tbk_request d = q;
+  d.kind = TBK_REQ_DOS;
+  d.precision = TBK_PREC_DD;
+  const Footprint base = footprint_of(d, L);          // one matrix built, rescaled and in ELL form
+  const int64_t Np = (L.total + 31) / 32 * 32;
+  const int64_t M = q.n_mom;
+  int rc = kubo_chunk(q.R);
+  auto total = [&](int c) {
+    const int64_t stores = 2 * M * (Np * c + 16) * 8;
+    const int64_t work = 12 * Np * c * 16;
+    return 4 * base.peak + stores + work + 4 * M * M * 16 + (64 << 20);
+  };
+  while (rc > 1 && (double)total(rc) > budget) rc >>= 1;
+  *chunk = rc;
+  Footprint f;
+  f.peak = total(rc);
+  f.resident = f.peak;
+  f.step_bytes = 0;
+  return f;
+}
+
 Footprint footprint_of(const tbk_request& q, const tbk_lattice_s& L) {
   const Cell& C = L.cell;
   const int64_t N = L.total;
@@ -464,6 +506,7 @@ struct SrvRequest {
   DevBuf sums;
   int64_t mu_off = -1;
   int32_t rc = 0, cs = 0, n_lanes = 0, n_steps = 0, s0 = 0, code = 0, n = 0, slab_rows = 0;
+  int32_t kubo_rc = 0;               // conductivity requests: vectors per stored chunk
   double step_bytes = 0.0;           // algorithmic bytes of one full step
   double mat_bytes = 0.0, vec_bytes = 0.0;
   std::vector<double> mu;
@@ -621,6 +664,44 @@ int build_request(tbk_server_s* S, SrvRequest* r) {
   return TBK_OK;
 }
 
+// A conductivity request end to end on the admission stream: H~, the
+// velocity commutators, mu_nm of tbk_kubo_mu with the stored blocks inside the
+// request's reservation.
+int run_kubo_request(tbk_server_s* S, SrvRequest* r) {
+  cudaStream_t st = S->st_admit;
+  const tbk_request& q = r->q;
+  tbk_sparse H = nullptr, Ht = nullptr, X[2] = {nullptr, nullptr}, V[2] = {nullptr, nullptr};
+  auto cleanup = [&] {
+    for (tbk_sparse m : {H, Ht, X[0], X[1], V[0], V[1]}) if (m) tbk_sparse_destroy(m);
+  };
+  int s = tbk_build_hamiltonian(&H, &r->lat, q.build_mode, q.extend, q.is_complex, st);
+  const double a = (q.e_max - q.e_min) / 2.0, b = (q.e_max + q.e_min) / 2.0;
+  if (s == TBK_OK) s = tbk_sparse_rescale(&Ht, H, a, b, st);
+  const int nops = q.kind == TBK_REQ_KUBO_BASTIN ? 2 : 1;
+  for (int k = 0; k < nops && s == TBK_OK; ++k) {
+    s = tbk_build_position(&X[k], &r->lat, q.axis[k], st);
+    if (s == TBK_OK) s = tbk_sparse_commutator(&V[k], Ht, X[k], st);   // X H~ - H~ X
+  }
+  if (s != TBK_OK) {
+    cleanup();
+    return s;
+  }
+  const int32_t M = q.n_mom;
+  r->mu.assign(2 * (size_t)M * M, 0.0);
+  const int32_t flags = TBK_MU_TENSOR | (q.precision == TBK_PREC_MIXED ? TBK_MU_MIXED_RECURSION
+                                         : q.precision == TBK_PREC_DD   ? TBK_MU_DD_RECURSION
+                                                                        : 0);
+  const double stores_gb = 2.0 * M * ((double)(Ht->ell.n_slices * 32) * r->kubo_rc + 16) * 8.0 / 1e9;
+  if (q.kind == TBK_REQ_KUBO_BASTIN)
+    s = tbk_kubo_mu(Ht, nullptr, nullptr, V[0], V[1], M, q.R, q.seed, nullptr, q.kernel, q.kernel_p0, q.kernel_p1,
+                    flags, stores_gb, r->mu.data(), st);
+  else
+    s = tbk_kubo_mu(Ht, V[0], V[0], nullptr, nullptr, M, q.R, q.seed, nullptr, q.kernel, q.kernel_p0, q.kernel_p1,
+                    flags, stores_gb, r->mu.data(), st);
+  cleanup();
+  return s;
+}
+
 void admit_main(tbk_server_s* S) {
   cudaSetDevice(S->dev);
   tl_async_alloc = &S->actx;
@@ -633,12 +714,12 @@ void admit_main(tbk_server_s* S) {
         if (S->queued.empty()) return false;
         SrvRequest* h = S->queued.front();
         return S->reserved + h->fp.peak <= (int64_t)S->budget && S->n_held < S->max_resident &&
-               S->arena.can_take(h->q.n_mom);
+               (h->q.kind != TBK_REQ_DOS || S->arena.can_take(h->q.n_mom));
       });
       if (S->stop) break;
       r = S->queued.front();
       S->queued.pop_front();
-      r->mu_off = S->arena.take(r->q.n_mom);
+      if (r->q.kind == TBK_REQ_DOS) r->mu_off = S->arena.take(r->q.n_mom);
       r->reserved = r->fp.peak;
       S->reserved += r->reserved;
       S->peak_reserved = std::max(S->peak_reserved, S->reserved);
@@ -650,9 +731,22 @@ void admit_main(tbk_server_s* S) {
     int s;
     {
       std::lock_guard<std::mutex> cap(S->capture_mu);
-      s = S->broken ? TBK_ERR_CUDA : build_request(S, r);
+      if (S->broken) s = TBK_ERR_CUDA;
+      else if (r->q.kind != TBK_REQ_DOS) s = run_kubo_request(S, r);
+      else s = build_request(S, r);
     }
     const std::string msg = s == TBK_OK ? std::string() : std::string(tbk_last_error());
+    if (r->q.kind != TBK_REQ_DOS) {                  // conductivity: done (or failed) here
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        r->t_ready = S->now_ms();
+        S->build_ms += r->t_ready - r->t_build0;
+        finish_request(S, r, s, s == TBK_OK ? std::string() : (S->broken ? S->broken_msg : msg));
+      }
+      S->cv_done.notify_all();
+      S->cv_admit.notify_all();
+      continue;
+    }
     {
       std::lock_guard<std::mutex> lk(S->mu);
       r->t_ready = S->now_ms();
@@ -1098,7 +1192,9 @@ extern "C" {
 
 int tbk_request_footprint(const tbk_request* req, int64_t* build_peak_bytes, int64_t* resident_bytes) {
   TBK_TRY(check_request(req));
-  const Footprint f = footprint_of(*req, *req->lattice);
+  int rc = 1;
+  const Footprint f = req->kind == TBK_REQ_DOS ? footprint_of(*req, *req->lattice)
+                                               : kubo_footprint(*req, *req->lattice, 120e9, &rc);
   if (build_peak_bytes) *build_peak_bytes = f.peak;
   if (resident_bytes) *resident_bytes = f.resident;
   return TBK_OK;
@@ -1205,14 +1301,21 @@ int tbk_server_submit(tbk_server S, const tbk_request* req, int64_t* ticket) {
   r->lat = *req->lattice;
   r->q = *req;
   r->q.lattice = nullptr;
-  r->fp = footprint_of(*req, r->lat);
+  if (req->kind == TBK_REQ_DOS) {
+    r->fp = footprint_of(*req, r->lat);
+  } else {
+    int rc = 1;
+    r->fp = kubo_footprint(*req, r->lat, S->budget, &rc);
+    r->kubo_rc = rc;
+  }
   std::lock_guard<std::mutex> lk(S->mu);
   if (S->broken) return fail(TBK_ERR_CUDA, "server failed: %s", S->broken_msg.c_str());
   if (S->stop) return fail(TBK_ERR_INVALID, "server stopped");
   if (r->fp.peak > (int64_t)S->budget)
     return fail(TBK_ERR_BUDGET, "request needs %lld bytes at its build peak, budget %.0f", (long long)r->fp.peak,
                 S->budget);
-  if (r->q.n_mom > S->arena_len) return fail(TBK_ERR_BUDGET, "n_mom %d exceeds the result arena", r->q.n_mom);
+  if (r->q.kind == TBK_REQ_DOS && r->q.n_mom > S->arena_len)
+    return fail(TBK_ERR_BUDGET, "n_mom %d exceeds the result arena", r->q.n_mom);
   r->ticket = S->next_ticket++;
   r->t_submit = S->now_ms();
   *ticket = r->ticket;

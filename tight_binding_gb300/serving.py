@@ -82,7 +82,9 @@ def request_footprint(lattice: PartialLattice, n_mom: int, R: int, precision: st
 
 
 class DosServer:
-    """Continuous-batching server of DoS moment requests on one GPU."""
+    """Continuous-batching server of DoS moment requests on one GPU; it also
+    takes conductivity (Kubo mu_nm) requests, which run as one solve each on
+    the admission stream while the DoS rounds go on."""
 
     def __init__(self, budget_gb: float = 120.0, steps_per_round: int = 16, autotune: bool = True,
                  max_resident: int = 4096, result_arena_mb: int = 64, step_gb: float = 2.0):
@@ -92,6 +94,7 @@ class DosServer:
         check(lib().tbk_server_create(C.byref(h), C.byref(cfg)))
         self._h = h
         self._n_mom: dict[int, int] = {}
+        self._kubo: set[int] = set()
 
     def submit(self, lattice: PartialLattice, n_mom: int, R: int, seed: int, e_min: float, e_max: float,
                precision: str = "mixed", mode: str = "periodic", extend: Sequence[int] | None = None,
@@ -103,17 +106,41 @@ class DosServer:
         self._n_mom[t.value] = int(n_mom)
         return int(t.value)
 
+    def submit_kubo(self, lattice: PartialLattice, kind: str, M: int, R: int, seed: int, e_min: float,
+                    e_max: float, axes=(0, 1), kernel=None, precision: str = "dd", mode: str = "periodic",
+                    extend: Sequence[int] | None = None, scalar=complex) -> int:
+        """Queues a conductivity request; poll returns g_m g_n mu_nm (M x M complex).
+        kind "bastin": mu_nm = <T_m r | v_a T_n v_b r> (conductivity_Kubo_Bastin);
+        "greenwood": mu_nm = <v_a T_m v_a r | T_n r> (conductivity_spectrum);
+        v_a = [x_a, H~] with H~ = (H - b)/a from e_min, e_max."""
+        from .kpm import Lorentz
+        kernel = kernel if kernel is not None else Lorentz(6.0)
+        q = _request(lattice, M, R, seed, e_min, e_max, precision, mode, extend, scalar)
+        q.kind = {"bastin": capi.REQ_KUBO_BASTIN, "greenwood": capi.REQ_KUBO_GREENWOOD}[kind]
+        q.axis[0], q.axis[1] = int(axes[0]), int(axes[1] if len(axes) > 1 else axes[0])
+        q.kernel, q.kernel_p0, q.kernel_p1 = kernel.kind, float(kernel.p0), float(kernel.p1)
+        t = C.c_int64()
+        check(lib().tbk_server_submit(self._h, C.byref(q), C.byref(t)))
+        self._n_mom[t.value] = int(M)
+        self._kubo.add(t.value)
+        return int(t.value)
+
     def poll(self, ticket: int, wait_ms: int = 0):
         """(mu, times_ms) when done, None while pending; raises TbkError if it failed.
-        times_ms = [queued, build, resident, total]."""
+        times_ms = [queued, build, resident, total].  Kubo requests: mu is the
+        M x M complex mu_nm."""
         n = self._n_mom[ticket]
-        mu = np.empty(n, dtype=np.float64)
+        kubo = ticket in self._kubo
+        mu = np.empty(2 * n * n if kubo else n, dtype=np.float64)
         times = np.zeros(4, dtype=np.float64)
         s = lib().tbk_server_poll(self._h, int(ticket), int(wait_ms), capi.ptr(mu), capi.ptr(times))
         if s == capi.TBK_PENDING:
             return None
         self._n_mom.pop(ticket, None)
+        self._kubo.discard(ticket)
         check(s)
+        if kubo:
+            mu = mu.view(np.complex128).reshape(n, n)
         return mu, times
 
     def result(self, ticket: int, timeout_s: float = 600.0):
@@ -134,7 +161,8 @@ class DosServer:
     def tuning(self) -> list[dict]:
         rows = np.zeros((64, 5), dtype=np.float64)
         k = lib().tbk_server_tuning(self._h, 64, capi.ptr(rows))
-        return [dict(precision="mixed" if r[0] == capi.PREC_MIXED else "fp64", width=int(r[1]), grid=int(r[2]),
+        names = {capi.PREC_MIXED: "mixed", capi.PREC_FP64: "fp64", capi.PREC_DD: "dd"}
+        return [dict(precision=names.get(int(r[0]), str(int(r[0]))), width=int(r[1]), grid=int(r[2]),
                      prefetch=int(r[3]), ms_per_step=float(r[4])) for r in rows[:max(k, 0)]]
 
     def close(self) -> None:
