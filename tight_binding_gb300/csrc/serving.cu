@@ -691,7 +691,8 @@ int run_kubo_request(tbk_server_s* S, SrvRequest* r) {
   const int32_t flags = TBK_MU_TENSOR | (q.precision == TBK_PREC_MIXED ? TBK_MU_MIXED_RECURSION
                                          : q.precision == TBK_PREC_DD   ? TBK_MU_DD_RECURSION
                                                                         : 0);
-  const double stores_gb = 2.0 * M * ((double)(Ht->ell.n_slices * 32) * r->kubo_rc + 16) * 8.0 / 1e9;
+  const double n_pad = (double)((Ht->rows + 31) / 32 * 32);
+  const double stores_gb = 2.0 * M * (n_pad * r->kubo_rc + 16) * 8.0 / 1e9;
   if (q.kind == TBK_REQ_KUBO_BASTIN)
     s = tbk_kubo_mu(Ht, nullptr, nullptr, V[0], V[1], M, q.R, q.seed, nullptr, q.kernel, q.kernel_p0, q.kernel_p1,
                     flags, stores_gb, r->mu.data(), st);
