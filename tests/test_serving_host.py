@@ -49,3 +49,18 @@ def test_server_needs_a_device(tb):
     with pytest.raises(tb.TbkError) as e:
         tb.DosServer(autotune=False)
     assert e.value.code == tb.capi.TBK_ERR_CUDA
+
+
+def test_conductivity_request_footprint_and_checks(tb):
+    """Conductivity requests: the footprint carries both stored block sides
+    (grows with M), is above the DoS footprint of the same lattice, and bad
+    axes are refused before any device work."""
+    X = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (256, 256))
+    dos, _ = tb.request_footprint(X, 512, 16, precision="dd")
+    k1, _ = tb.request_footprint(X, 512, 16, precision="dd", kind="bastin")
+    k2, _ = tb.request_footprint(X, 1024, 16, precision="dd", kind="bastin")
+    assert k1 > dos and k2 > k1
+    stores = 2 * 512 * 65536 * 16 * 8
+    assert k1 >= stores
+    with pytest.raises(tb.TbkError, match="axis out of range"):
+        tb.request_footprint(X, 64, 4, kind="greenwood", axes=(2,))

@@ -72,10 +72,19 @@ def _request(lattice: PartialLattice, n_mom: int, R: int, seed: int, e_min: floa
     return q
 
 
+KINDS = {"dos": capi.REQ_DOS, "bastin": capi.REQ_KUBO_BASTIN, "greenwood": capi.REQ_KUBO_GREENWOOD}
+
+
 def request_footprint(lattice: PartialLattice, n_mom: int, R: int, precision: str = "mixed",
-                      e_min: float = -1.0, e_max: float = 1.0, **kw) -> tuple[int, int]:
-    """(build peak bytes, resident bytes) that admission charges for a request."""
+                      e_min: float = -1.0, e_max: float = 1.0, kind: str = "dos", axes=(0, 1),
+                      **kw) -> tuple[int, int]:
+    """(build peak bytes, resident bytes) that admission charges for a request
+    (conductivity kinds: at the 120 GB default budget)."""
     q = _request(lattice, n_mom, R, 0, e_min, e_max, precision, **kw)
+    q.kind = KINDS[kind]
+    if kind != "dos":
+        q.axis[0], q.axis[1] = int(axes[0]), int(axes[1] if len(axes) > 1 else axes[0])
+        q.kernel = capi.KERNEL_LORENTZ
     peak, res = C.c_int64(), C.c_int64()
     check(lib().tbk_request_footprint(C.byref(q), C.byref(peak), C.byref(res)))
     return int(peak.value), int(res.value)
