@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <mutex>
 #include <vector>
 
 #include "kpm_device.cuh"
@@ -225,7 +226,8 @@ __global__ void greenwood_kernel(const double2* __restrict__ mu, int32_t M, cons
 
 // timing of the last tbk_kubo_mu call (CUDA events on the caller's stream)
 struct KuboTiming { double ms_blocks = 0, ms_gemm = 0, gemm_flops = 0, block_bytes = 0; int chunks = 0; };
-KuboTiming g_kubo_timing;
+KuboTiming g_kubo_timing;        // the last solve's timing (calls may come from several threads)
+std::mutex g_kubo_timing_mu;
 
 int pick_chunk(int R) {
   int c = 1;
@@ -489,7 +491,10 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     tm.chunks += 1;
   }
   for (auto& e : ev) cudaEventDestroy(e);
-  g_kubo_timing = tm;
+  {
+    std::lock_guard<std::mutex> lk(g_kubo_timing_mu);
+    g_kubo_timing = tm;
+  }
   // kernel factors g_m g_n (FP64)
   std::vector<double> g(M);
   TBK_TRY(tbk_kernel_seq(kernel_kind, M, kp0, kp1, g.data()));
@@ -552,16 +557,24 @@ int tbk_mu_from_blocks(int32_t M, int64_t K, const double* L, const double* Rb, 
   tm.gemm_flops = 8.0 * M * (double)M * (double)K * ((flags & TBK_MU_TENSOR) ? 3.0 : 1.0);
   tm.block_bytes = 2.0 * M * (double)K * 8.0;
   tm.chunks = 1;
-  g_kubo_timing = tm;
+  {
+    std::lock_guard<std::mutex> lk(g_kubo_timing_mu);
+    g_kubo_timing = tm;
+  }
   return TBK_OK;
 }
 
 int tbk_kubo_last_timing(double* ms_blocks, double* ms_gemm, double* gemm_flops, double* block_bytes, int32_t* chunks) {
-  if (ms_blocks) *ms_blocks = g_kubo_timing.ms_blocks;
-  if (ms_gemm) *ms_gemm = g_kubo_timing.ms_gemm;
-  if (gemm_flops) *gemm_flops = g_kubo_timing.gemm_flops;
-  if (block_bytes) *block_bytes = g_kubo_timing.block_bytes;
-  if (chunks) *chunks = g_kubo_timing.chunks;
+  KuboTiming t;
+  {
+    std::lock_guard<std::mutex> lk(g_kubo_timing_mu);
+    t = g_kubo_timing;
+  }
+  if (ms_blocks) *ms_blocks = t.ms_blocks;
+  if (ms_gemm) *ms_gemm = t.ms_gemm;
+  if (gemm_flops) *gemm_flops = t.gemm_flops;
+  if (block_bytes) *block_bytes = t.block_bytes;
+  if (chunks) *chunks = t.chunks;
   return TBK_OK;
 }
 
