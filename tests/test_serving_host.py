@@ -64,3 +64,15 @@ def test_conductivity_request_footprint_and_checks(tb):
     assert k1 >= stores
     with pytest.raises(tb.TbkError, match="axis out of range"):
         tb.request_footprint(X, 64, 4, kind="greenwood", axes=(2,))
+
+
+def test_unknown_request_kind_is_refused(tb):
+    import ctypes as C
+    from tight_binding_gb300 import capi
+    from tight_binding_gb300.serving import _request
+    X = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (8, 8))
+    q = _request(X, 16, 2, 0, -4.1, 4.1)
+    q.kind = 7
+    a, b = C.c_int64(), C.c_int64()
+    assert capi.lib().tbk_request_footprint(C.byref(q), C.byref(a), C.byref(b)) == capi.TBK_ERR_INVALID
+    assert b"unknown request kind" in capi.lib().tbk_last_error()
