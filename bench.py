@@ -686,7 +686,8 @@ def run_small(args):
     ref_mu = None
     for name, prec, extra in (("fp64", "fp64", 0), ("fp64_no_graph", "fp64", capi.FLAG_NO_GRAPH),
                               ("fp64_cluster", "fp64", capi.FLAG_PERSISTENT), ("mixed", "mixed", 0),
-                              ("mixed_cluster", "mixed", capi.FLAG_PERSISTENT), ("dd", "dd", 0)):
+                              ("mixed_cluster", "mixed", capi.FLAG_PERSISTENT),
+                              ("mixed_two_step", "mixed", capi.FLAG_TWO_STEP), ("dd", "dd", 0)):
         sol = tb.KpmSolver(Ht, R, precision=prec, doubling=True, flags=capi.FLAG_DEVICE_PTRS | extra)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * steps)]
         for _ in range(args.warmup + 2):
