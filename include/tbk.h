@@ -162,6 +162,16 @@ int tbk_build_hamiltonian(tbk_sparse* out, tbk_lattice lat, int32_t mode,
                           const int32_t* extend, int32_t is_complex, void* stream);
 /* op_position(axis), TB/lattice.h:313-336: the diagonal X as a sparse matrix. */
 int tbk_build_position(tbk_sparse* out, tbk_lattice lat, int32_t axis, void* stream);
+/* Bond-displacement velocity: the matrix of tbk_build_hamiltonian with every
+ * hopping entry (row i, column j) multiplied by scale * (r_i - r_j)_axis taken
+ * along the bond itself (the hop's lattice vector), so bonds across a periodic
+ * boundary get their short displacement; on-site terms and the scalar field
+ * drop out.  With scale = 1/a it equals [X, H~] (op_velocity / the Kubo
+ * drivers' X H~ - H~ X, TB/lattice.h:338-345, TB/snippets.h:316-317) on every
+ * bond that does not wrap, and stays translation invariant where [X, H~]
+ * jumps by the box length.  No factor i, as the reference's commutator. */
+int tbk_build_velocity_bond(tbk_sparse* out, tbk_lattice lat, int32_t mode, const int32_t* extend,
+                            int32_t is_complex, int32_t axis, double scale, void* stream);
 /* Wraps a CSC (Eigen compressed layout).  device_ptrs: arrays already on the GPU. */
 int tbk_sparse_from_csc(tbk_sparse* out, int32_t rows, int32_t cols, int64_t nnz,
                         const int32_t* col_ptr, const int32_t* row_idx,

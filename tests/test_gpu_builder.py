@@ -223,3 +223,39 @@ def test_builder_every_site_removed(gpu):
                                   removed=X.removed_sites().astype(np.int32)))
     _assert_same(H, ref)
     assert H.to_csc()[0][-1] == 0
+
+
+def _scipy_csc(M):
+    import scipy.sparse as sp
+    cp, ri, v = M.to_csc()
+    n = len(cp) - 1
+    return sp.csc_matrix((v, ri, cp), shape=(n, n))
+
+
+def test_bond_velocity_matches_commutator_without_wrap(gpu):
+    """Open boundaries: the bond-displacement velocity (scale 1/a) equals
+    X H~ - H~ X entry by entry (complex gauge, disorder, two-atom cell)."""
+    tb = gpu
+    X = tb.PartialLattice(tb.Honeycomb().add_hopping("A", 1, -2.7), (9, 7))
+    X.set_gauge_linear(*landau_gauge(0.05))
+    X.set_scalar_disorder(0.8, 2)
+    H = X.get_Hamiltonian_sparse(complex)
+    G = tb.GreenFunction(8, H, -8.6, 8.6)
+    for axis in (0, 1):
+        comm = _scipy_csc(tb.commutator(G.scaled_HE, X.op_position(axis))).toarray()
+        bond = _scipy_csc(X.op_velocity_bond(axis, scalar=complex, scale=1.0 / G.a, mode="sparse")).toarray()
+        assert np.max(np.abs(comm - bond)) <= 1e-14 * np.max(np.abs(comm))
+
+
+def test_bond_velocity_periodic_is_translation_invariant(gpu):
+    """Periodic square lattice: every bond carries +-t (scale 1) along its own
+    displacement, including the wrapping bonds where [X, H] jumps by L - 1."""
+    tb = gpu
+    X = tb.PartialLattice(tb.Square().add_hopping("A", 1, 1.0), (6, 5))
+    V = _scipy_csc(X.op_velocity_bond(0, extend=[1, 1], scalar=float)).toarray()
+    assert set(np.unique(np.round(V, 12))) == {-1.0, 0.0, 1.0}
+    assert np.allclose(V, -V.T)
+    assert np.allclose(V.sum(axis=0), 0.0)
+    H = X.get_Hamiltonian_periodic_extend_bare_sparse([1, 1], float)
+    comm = _scipy_csc(tb.commutator(H, X.op_position(0))).toarray()
+    assert np.max(np.abs(comm)) == pytest.approx(5.0)         # the wrap: x jumps by L - 1

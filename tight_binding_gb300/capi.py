@@ -110,6 +110,7 @@ SIGNATURES = {
     "tbk_lattice_kept_number": (C.c_int, [_vp, _pi64]),
     "tbk_build_hamiltonian": (C.c_int, [C.POINTER(_vp), _vp, _i32, _pi32, _i32, _vp]),
     "tbk_build_position": (C.c_int, [C.POINTER(_vp), _vp, _i32, _vp]),
+    "tbk_build_velocity_bond": (C.c_int, [C.POINTER(_vp), _vp, _i32, _pi32, _i32, _i32, C.c_double, _vp]),
     "tbk_sparse_from_csc": (C.c_int, [C.POINTER(_vp), _i32, _i32, _i64, _vp, _vp, _vp, _i32, _i32, _vp]),
     "tbk_sparse_info": (C.c_int, [_vp, _pi32, _pi32, _pi64, _pi32]),
     "tbk_sparse_download": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),

@@ -213,6 +213,8 @@ struct BuildParams {
   const int32_t* comp;          // bare -> compressed (-1 removed), or null
   const int32_t* inv;           // compressed -> bare, or null
   int32_t* warn_flag;           // imaginary part discarded (real Scalar)
+  int32_t vel_axis;             // >= 0: bond-displacement velocity along this axis instead of H
+  double vel_scale;
 };
 
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
@@ -269,6 +271,15 @@ struct Cand {
 };
 
 // Enumerates the triplets of CSC column j; returns the count (or -1 on overflow).
+// component vel_axis of the hop's bond vector r_to - r_from (minimum image:
+// the hop's own lattice vector, whatever the periodic wrap)
+__device__ double bond_component(const BuildParams& P, const DevHop& h) {
+  const int x = P.vel_axis;
+  double s = 0.0;
+  for (int c = 0; c < P.dim; ++c) s = dadd(s, dmul(P.bases[c * 3 + x], (double)h.v[c]));
+  return dadd(dadd(-P.pos[h.from * 3 + x], s), P.pos[h.to * 3 + x]);
+}
+
 __device__ int column_candidates(const BuildParams& P, int32_t j, Cand* c, bool want_values) {
   if (j >= P.n_kept) return 0;
   int64_t bare = P.inv ? P.inv[j] : j;
@@ -305,7 +316,13 @@ __device__ int column_candidates(const BuildParams& P, int32_t j, Cand* c, bool 
           c[n].key = (lin * P.n_hops + hi) * 2;
           if (want_values) {
             double tr, ti;
-            hop_value(P, h, iv, rb, rb == bare, tr, ti);
+            const bool vel = P.vel_axis >= 0;
+            hop_value(P, h, iv, rb, !vel && rb == bare, tr, ti);
+            if (vel) {                                   // (x_row - x_col) t with row = from, col = to
+              const double f = dmul(-bond_component(P, h), P.vel_scale);
+              tr = dmul(tr, f);
+              ti = dmul(ti, f);
+            }
             if (!P.is_complex) { if (fabs(ti) > 1e-10) atomicOr(P.warn_flag, 1); ti = 0.0; }
             c[n].re = tr;
             c[n].im = ti;
@@ -337,6 +354,11 @@ __device__ int column_candidates(const BuildParams& P, int32_t j, Cand* c, bool 
         if (want_values) {
           double tr, ti;
           hop_value(P, h, cj, bare, false, tr, ti);
+          if (P.vel_axis >= 0) {                         // row = to, col = from: + bond
+            const double f = dmul(bond_component(P, h), P.vel_scale);
+            tr = dmul(tr, f);
+            ti = dmul(ti, f);
+          }
           if (!P.is_complex) { if (fabs(ti) > 1e-10) atomicOr(P.warn_flag, 1); ti = 0.0; }
           c[n].re = tr;
           c[n].im = -ti;
@@ -699,8 +721,8 @@ int tbk_device_count(void) {
   return n;
 }
 
-int tbk_build_hamiltonian(tbk_sparse* out, tbk_lattice L, int32_t mode, const int32_t* extend,
-                          int32_t is_complex, void* stream) {
+static int build_matrix(tbk_sparse* out, tbk_lattice L, int32_t mode, const int32_t* extend, int32_t is_complex,
+                        int32_t vel_axis, double vel_scale, void* stream) {
   if (!out || !L) return fail(TBK_ERR_INVALID, "tbk_build_hamiltonian: null argument");
   *out = nullptr;
   if (mode < 0 || mode > 2) return fail(TBK_ERR_INVALID, "unknown build mode %d", mode);
@@ -709,6 +731,8 @@ int tbk_build_hamiltonian(tbk_sparse* out, tbk_lattice L, int32_t mode, const in
   if (C.hops.empty()) { /* "Warning: no hopping is added!" — an all-zero matrix */ }
   BuildParams P;
   memset(&P, 0, sizeof(P));
+  P.vel_axis = vel_axis;
+  P.vel_scale = vel_scale;
   P.dim = C.dim;
   P.n_atoms = C.n_atoms;
   P.n_hops = (int32_t)C.hops.size();
@@ -794,6 +818,18 @@ int tbk_build_hamiltonian(tbk_sparse* out, tbk_lattice L, int32_t mode, const in
   if (e != cudaSuccess) { delete A; return fail(TBK_ERR_CUDA, "builder: %s", cudaGetErrorString(e)); }
   *out = A;
   return TBK_OK;
+}
+
+int tbk_build_hamiltonian(tbk_sparse* out, tbk_lattice L, int32_t mode, const int32_t* extend,
+                          int32_t is_complex, void* stream) {
+  return build_matrix(out, L, mode, extend, is_complex, -1, 0.0, stream);
+}
+
+int tbk_build_velocity_bond(tbk_sparse* out, tbk_lattice L, int32_t mode, const int32_t* extend, int32_t is_complex,
+                            int32_t axis, double scale, void* stream) {
+  if (!L) return fail(TBK_ERR_INVALID, "tbk_build_velocity_bond: null argument");
+  if (axis < 0 || axis >= L->cell.dim) return fail(TBK_ERR_INVALID, "Error: axis out of range.");
+  return build_matrix(out, L, mode, extend, is_complex, axis, scale, stream);
 }
 
 int tbk_build_position(tbk_sparse* out, tbk_lattice L, int32_t axis, void* stream) {

@@ -104,15 +104,21 @@ def bastin_integrate(eps, zeta):
 
 def conductivity_Kubo_Bastin(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMatrix, N: int, E_min: float,
                              E_max: float, Volume: float = 1.0, R: int = 4, seed: int = 0, kernel: Kernel | None = None,
-                             tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd", fuse_ops: bool = False):
+                             tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd", fuse_ops: bool = False,
+                             velocity=None):
     """TB/snippets.h:306-456: G(N, H, E_min-1e-8, E_max+1e-8); v = X H~ - H~ X;
     aL = g T r, aR = g v_x T v_y r; zeta at the N Chebyshev nodes; cumulative
-    integral from E = 0.  Returns dict with eps, zeta, E, sigma_re, sigma_im, mu."""
+    integral from E = 0.  Returns dict with eps, zeta, E, sigma_re, sigma_im, mu.
+    velocity: optional callable G -> (v_x, v_y) replacing the commutators (e.g.
+    the bond-displacement form, PartialLattice.op_velocity_bond with scale 1/G.a)."""
     kernel = kernel if kernel is not None else Lorentz(6.0)
     G = GreenFunction(N, H_og, E_min - 1e-8, E_max + 1e-8)
     Ht = G.scaled_HE
-    v_x = commutator(Ht, op_x)
-    v_y = commutator(Ht, op_y)
+    if velocity is not None:
+        v_x, v_y = velocity(G)
+    else:
+        v_x = commutator(Ht, op_x)
+        v_y = commutator(Ht, op_y)
     mu = kubo_mu(Ht, None, None, v_x, v_y, N, R, seed, kernel=kernel, tensor=tensor, budget_gb=budget_gb,
                  recursion=recursion, fuse_ops=fuse_ops)
     eps = chebyshev_nodes(N)

@@ -297,6 +297,22 @@ class PartialLattice:
         check(lib().tbk_build_position(C.byref(h), self._h, int(axis), None))
         return SparseMatrix(h.value)
 
+    def op_velocity_bond(self, axis: int, extend=None, scalar=complex, scale: float = 1.0,
+                         mode: str = "periodic") -> SparseMatrix:
+        """Bond-displacement velocity along `axis`: the Hamiltonian of `mode`
+        ("periodic" with `extend`, "sparse" or "bare") with each hopping entry
+        (i, j) times scale * (r_i - r_j) along the bond itself.  scale = 1/a
+        gives [X, H~] on every bond that does not cross a periodic boundary
+        (and the short displacement on those that do)."""
+        ext = np.zeros(3, dtype=np.int32)
+        if extend is not None:
+            ext[: self.dim] = extend
+        m = {"periodic": capi.BUILD_PERIODIC_BARE, "sparse": capi.BUILD_SPARSE, "bare": capi.BUILD_BARE}[mode]
+        h = C.c_void_p()
+        check(lib().tbk_build_velocity_bond(C.byref(h), self._h, m, capi.as_i32p(ext), int(scalar is complex),
+                                            int(axis), float(scale), None))
+        return SparseMatrix(h.value)
+
     def op_velocity(self, axis: int) -> SparseMatrix:
         """X H - H X with the real open-boundary H (no factor i), TB/lattice.h:338-345."""
         return commutator(self.get_Hamiltonian_sparse(float), self.op_position(axis))
