@@ -220,6 +220,17 @@ class PartialLattice {
     check(tbk_sparse_commutator(&h, H.handle(), X.handle(), nullptr));
     return SparseMatrix(h);
   }
+  // bond-displacement velocity (periodic axes as in `periodic`): each hopping
+  // times scale * (r_i - r_j) along its own bond; scale = 1/a gives [X, H~]
+  // wherever a bond does not wrap
+  template <class Scalar>
+  SparseMatrix op_velocity_bond(int axis, LatticeVector<Dim> periodic, double scale = 1.0) {
+    int32_t ext[3] = {0, 0, 0};
+    for (int i = 0; i < Dim; ++i) ext[i] = periodic[i];
+    tbk_sparse h = nullptr;
+    check(tbk_build_velocity_bond(&h, h_, TBK_BUILD_PERIODIC_BARE, ext, is_cplx<Scalar>(), axis, scale, nullptr));
+    return SparseMatrix(h);
+  }
   tbk_lattice handle() const { return h_; }
 
  private:
