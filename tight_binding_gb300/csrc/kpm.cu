@@ -191,7 +191,7 @@ static int tma_setup(int R, bool braket, int smem, int* occ) {
 }
 
 static int rows_per_tile(int prec, int Rc) {
-  int vpl = prec == TBK_PREC_MIXED ? (Rc >= 2 ? 2 : 1) : 1;
+  int vpl = (prec == TBK_PREC_MIXED || prec == TBK_PREC_DD) ? (Rc >= 2 ? 2 : 1) : 1;
   int lpr = Rc / vpl;
   return (32 / lpr) * kStepWarps;
 }

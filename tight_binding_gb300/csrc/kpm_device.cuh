@@ -95,8 +95,11 @@ template <typename F, int VPL>
 __device__ __forceinline__ LaneV<F, VPL> ld_ro(const typename C2<F>::T* p) {
   LaneV<F, VPL> o;
   if constexpr (is_dd<F>) {
-    float4 q = __ldg(reinterpret_cast<const float4*>(p));
-    o.re[0] = dd(q.x, q.y); o.im[0] = dd(q.z, q.w);
+#pragma unroll
+    for (int v = 0; v < VPL; ++v) {
+      float4 q = __ldg(reinterpret_cast<const float4*>(p) + v);
+      o.re[v] = dd(q.x, q.y); o.im[v] = dd(q.z, q.w);
+    }
   } else if constexpr (sizeof(F) == 4 && VPL == 2) {
     float4 q = __ldg(reinterpret_cast<const float4*>(p));
     o.re[0] = q.x; o.im[0] = q.y; o.re[1] = q.z; o.im[1] = q.w;
@@ -110,8 +113,11 @@ template <typename F, int VPL>
 __device__ __forceinline__ LaneV<F, VPL> ld_stream(const typename C2<F>::T* p) {
   LaneV<F, VPL> o;
   if constexpr (is_dd<F>) {
-    float4 q = __ldcs(reinterpret_cast<const float4*>(p));
-    o.re[0] = dd(q.x, q.y); o.im[0] = dd(q.z, q.w);
+#pragma unroll
+    for (int v = 0; v < VPL; ++v) {
+      float4 q = __ldcs(reinterpret_cast<const float4*>(p) + v);
+      o.re[v] = dd(q.x, q.y); o.im[v] = dd(q.z, q.w);
+    }
   } else if constexpr (sizeof(F) == 4 && VPL == 2) {
     float4 q = __ldcs(reinterpret_cast<const float4*>(p));
     o.re[0] = q.x; o.im[0] = q.y; o.re[1] = q.z; o.im[1] = q.w;
@@ -124,7 +130,9 @@ __device__ __forceinline__ LaneV<F, VPL> ld_stream(const typename C2<F>::T* p) {
 template <typename F, int VPL>
 __device__ __forceinline__ void st_v(typename C2<F>::T* p, const LaneV<F, VPL>& v) {
   if constexpr (is_dd<F>) {
-    *reinterpret_cast<float4*>(p) = make_float4(v.re[0].hi, v.re[0].lo, v.im[0].hi, v.im[0].lo);
+#pragma unroll
+    for (int u = 0; u < VPL; ++u)
+      reinterpret_cast<float4*>(p)[u] = make_float4(v.re[u].hi, v.re[u].lo, v.im[u].hi, v.im[u].lo);
   } else if constexpr (sizeof(F) == 4 && VPL == 2) {
     *reinterpret_cast<float4*>(p) = make_float4(v.re[0], v.im[0], v.re[1], v.im[1]);
   } else {
@@ -227,7 +235,9 @@ __device__ __forceinline__ void finish_acc(LaneV<F, VPL>& acc) {
 }
 
 template <typename F> struct VecW { static constexpr int max_vpl = (sizeof(F) == 4) ? 2 : 1; };
-template <> struct VecW<dd> { static constexpr int max_vpl = 1; };
+// double-float: two vectors per lane (two 16-byte accesses) as for complex64,
+// twice the rows per warp and so twice the gathers in flight per warp
+template <> struct VecW<dd> { static constexpr int max_vpl = 2; };
 
 // Asynchronous bulk prefetch of [src, src+bytes) into L2 (no shared memory, no
 // completion to wait for); bytes % 16 == 0 and src 16-byte aligned.
