@@ -484,9 +484,12 @@ int tbk_server_tuning(tbk_server server, int32_t max_rows, double* rows);
  * mu_out is a device array of n_mom doubles, ready when `stream` completes.
  * Work space is a fixed file-scope device array of 32.06 MiB: N * R must not
  * exceed 1,048,576 (larger sizes fail with TBK_ERR_INVALID).  Calls share that
- * array, so calls that overlap on the GPU race; the first call on a device
- * looks up the array's address and should come before any stream capture.
- * Nothing is allocated or freed. */
+ * array, so calls that overlap on the GPU race.  The CUDA runtime loads device
+ * code lazily, so the first call on each device loads the module and reserves
+ * the 32.06 MiB array then (it fails with TBK_ERR_CUDA if the device is full):
+ * make that call during set-up, before any stream capture.  From then on the
+ * array stays reserved on that device until exit and calls allocate and free
+ * nothing. */
 int tbk_cheb_moments_noalloc(int32_t n_rows, const int32_t* row_ptr, const int32_t* col_idx,
                              const double* values, int32_t is_complex, int32_t n_mom,
                              const double* bras, const double* kets, int32_t R, double* mu_out,

@@ -12,15 +12,20 @@
 //
 // Limits and sharing: the array holds two work blocks of at most
 // kNoAllocMaxEntries complex128 values each (N * R <= 1,048,576) plus the
-// partial sums, 32.06 MiB in total, and every GPU that loads the library keeps
-// it until the process exits.  All calls share it: two calls whose work
-// overlaps on the GPU (different streams, or different host threads) race on
-// the same scratch and give wrong results; serialise them.  The first call on a
-// device looks up the array's device address (cudaGetSymbolAddress) for that
-// device; make that first call before capturing any stream.
+// partial sums, 32.06 MiB in total.  The CUDA runtime loads a library's device
+// code lazily (the default since CUDA 12.2), so the array is not reserved when
+// the library is loaded: the first call on each device loads this file's module
+// and reserves the 32.06 MiB then, and can fail for lack of memory if the
+// device is already full.  Make that first call during set-up, before the
+// memory budget is handed out and before capturing any stream; after it the
+// array stays reserved on that device until the process exits and later calls
+// allocate nothing.  All calls share the array: two calls whose work overlaps
+// on the GPU (different streams, or different host threads) race on the same
+// scratch and give wrong results; serialise them.  Each call looks up the
+// array's device address on the current device (cudaGetSymbolAddress, a
+// lookup once the module is loaded), so a context that was reset and created
+// again is never handed a stale address.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "tbk_internal.h"
 
@@ -35,24 +40,13 @@ constexpr size_t kNoAllocBytes = 2 * size_t(kNoAllocMaxEntries) * sizeof(double2
 // The scratch: [block A][block B][partials: 2 x kNoAllocGrid doubles].
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kMaxDevices] = {nullptr};
-
-// Device address of the scratch on the current device (looked up once per device).
+// Device address of the scratch on the current device.
 int noalloc_scratch(void** out) {
-  int dev = 0;
-  TBK_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return fail(TBK_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(TBK_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(TBK_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
+  *out = p;
   return TBK_OK;
 }
 
@@ -65,34 +59,38 @@ __global__ void noalloc_copy_kernel(int64_t total, const double2* __restrict__ s
 // One recursion step on CSR rows, vectors column-major (index i + r*N):
 //   first: y = H x                    else: y = 2 H x - y
 //   part[b] = sum Re <bras|y>;  first also part[grid + b] = sum Re <bras|x>.
+// Threads walk rows grid-stride (consecutive threads, consecutive rows of one
+// vector: coalesced); each thread runs the row for every vector in turn.
 __global__ void __launch_bounds__(kNoAllocThreads) noalloc_step_kernel(
     int32_t n, int32_t R, const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col_idx,
     const double* __restrict__ vals, int cplx, const double2* __restrict__ x, double2* __restrict__ y,
     const double2* __restrict__ bras, int first, double* __restrict__ part) {
-  const int64_t total = (int64_t)n * R;
   double m0 = 0.0, m1 = 0.0;
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t i = (int32_t)(g % n);
-    const int64_t base = g - i;   // r * N
-    double ar = 0.0, ai = 0.0;
-    for (int32_t p = row_ptr[i]; p < row_ptr[i + 1]; ++p) {
-      const double2 xv = x[base + col_idx[p]];
-      if (cplx) {
-        const double hr = vals[2 * p], hi = vals[2 * p + 1];
-        ar += hr * xv.x - hi * xv.y;
-        ai += hr * xv.y + hi * xv.x;
-      } else {
-        ar += vals[p] * xv.x;
-        ai += vals[p] * xv.y;
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int32_t p0 = row_ptr[i], p1 = row_ptr[i + 1];
+    for (int32_t r = 0; r < R; ++r) {
+      const int64_t base = (int64_t)r * n;
+      const int64_t g = base + i;
+      double ar = 0.0, ai = 0.0;
+      for (int32_t p = p0; p < p1; ++p) {
+        const double2 xv = x[base + col_idx[p]];
+        if (cplx) {
+          const double hr = vals[2 * p], hi = vals[2 * p + 1];
+          ar += hr * xv.x - hi * xv.y;
+          ai += hr * xv.y + hi * xv.x;
+        } else {
+          ar += vals[p] * xv.x;
+          ai += vals[p] * xv.y;
+        }
       }
+      double2 out;
+      if (first) { out.x = ar; out.y = ai; }
+      else { const double2 pv = y[g]; out.x = 2.0 * ar - pv.x; out.y = 2.0 * ai - pv.y; }
+      y[g] = out;
+      const double2 b = bras[g];
+      m0 += b.x * out.x + b.y * out.y;
+      if (first) { const double2 xs = x[g]; m1 += b.x * xs.x + b.y * xs.y; }
     }
-    double2 out;
-    if (first) { out.x = ar; out.y = ai; }
-    else { const double2 pv = y[g]; out.x = 2.0 * ar - pv.x; out.y = 2.0 * ai - pv.y; }
-    y[g] = out;
-    const double2 b = bras[g];
-    m0 += b.x * out.x + b.y * out.y;
-    if (first) { const double2 xs = x[g]; m1 += b.x * xs.x + b.y * xs.y; }
   }
   __shared__ double sh[2][kNoAllocThreads / 32];
   for (int o = 16; o > 0; o >>= 1) {
