@@ -179,6 +179,16 @@ int tbk_sparse_from_csc(tbk_sparse* out, int32_t rows, int32_t cols, int64_t nnz
                         void* stream);
 int tbk_sparse_info(tbk_sparse A, int32_t* rows, int32_t* cols, int64_t* nnz,
                     int32_t* is_complex);
+/* Row classes of the recursion form (no counterpart in the reference, whose
+ * cuSPARSE path always reads column indices).  When every row's off-diagonal
+ * entries repeat one of at most 255 lists of (column - row, value) — a lattice
+ * Hamiltonian without vacancies whose hoppings are the same in every cell —
+ * the recursion kernels compute neighbours from a small per-class table
+ * instead of loading the ELL's columns and values.  Examines A once (exact:
+ * every row is compared with its class) and returns the class count, 0 when
+ * the matrix does not qualify.  The environment variable TBK_NO_CLASSES=1,
+ * read when a matrix is first examined, keeps the ELL form (A/B comparisons). */
+int tbk_sparse_row_classes(tbk_sparse A, int32_t* n_classes, void* stream);
 /* Copies the CSC arrays to host buffers. */
 int tbk_sparse_download(tbk_sparse A, int32_t* col_ptr, int32_t* row_idx, double* values,
                         void* stream);

@@ -190,6 +190,42 @@ def test_config_sizes_counts(gpu):
     assert H3.nnz == counts["fcc_128_pbc_disorder"]["nnz_H"]
 
 
+CONFIG_SYSTEMS = {
+    # name: (cell factory, span, extend, complex, disorder (W, seed), Landau B, rescale bounds)
+    "honeycomb_1024_pbc_disorder": (lambda tb: tb.Honeycomb().add_hopping("A", 1, -2.7), (1024, 1024), [1, 1],
+                                    False, (1.0, 1), None, (-8.7, 8.7)),
+    "square_256_openx_pbcy_landau": (lambda tb: tb.Square().add_hopping("A", 1, 1.0), (256, 256), [0, 1], True,
+                                     None, 2 * np.pi / 64, (-4.0, 4.0)),
+    "fcc_128_pbc_disorder": (lambda tb: tb.FCC().add_hopping("A", 1, 1.0), (128, 128, 128), [1, 1, 1], False,
+                             (2.0, 4), None, (-13.0, 13.0)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CONFIG_SYSTEMS))
+def test_config_sizes_full_arrays(gpu, name):
+    """The benchmark lattices at full size: every col_ptr / row_idx entry of H
+    and of H~ = (H - bI)/a bit-exact with the oracle; values bit-exact, except
+    the Landau-gauge phases (device cos/sin against libm), which agree to 4e-16
+    absolute (|t| = 1)."""
+    tb = gpu
+    mk, span, extend, cplx, disorder, B, (lo, hi) = CONFIG_SYSTEMS[name]
+    cell = mk(tb)
+    H, ref = _build_both(tb, cell, span, "periodic", cplx, extend=extend,
+                         gauge=landau_gauge(B) if B is not None else None, disorder=disorder)
+    cp, ri, v = H.to_csc()
+    assert np.array_equal(cp, ref[0]) and np.array_equal(ri, ref[1])
+    if B is None:
+        assert np.array_equal(v, ref[2])
+    else:
+        assert np.max(np.abs(v - ref[2])) <= 4e-16
+    G = tb.GreenFunction(8, H, lo, hi)
+    got = G.scaled_HE.to_csc()
+    # the oracle rescales the device's own values, so the rescale itself is checked bit for bit
+    want = orc.rescale_csc(len(cp) - 1, cp, ri, v, G.a, G.b)
+    for x, y in zip(got, want):
+        assert np.array_equal(x, y)
+
+
 def test_builder_random_vacancies_device_compaction(gpu):
     """remove_atoms_random on both sublattices of a 256 x 192 honeycomb: the
     device prefix-sum compaction gives the oracle's index_c build bit-exact."""

@@ -113,6 +113,7 @@ SIGNATURES = {
     "tbk_build_velocity_bond": (C.c_int, [C.POINTER(_vp), _vp, _i32, _pi32, _i32, _i32, C.c_double, _vp]),
     "tbk_sparse_from_csc": (C.c_int, [C.POINTER(_vp), _i32, _i32, _i64, _vp, _vp, _vp, _i32, _i32, _vp]),
     "tbk_sparse_info": (C.c_int, [_vp, _pi32, _pi32, _pi64, _pi32]),
+    "tbk_sparse_row_classes": (C.c_int, [_vp, _pi32, _vp]),
     "tbk_sparse_download": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "tbk_sparse_destroy": (None, [_vp]),
     "tbk_sparse_rescale": (C.c_int, [C.POINTER(_vp), _vp, _d, _d, _vp]),

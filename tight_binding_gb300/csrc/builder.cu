@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -692,6 +693,242 @@ int ensure_ell_dd(tbk_sparse_s* A, cudaStream_t st) {
   return TBK_OK;
 }
 
+// ------------------------------------------------------------- row classes
+// A row's class key: its number of off-diagonal entries and, in ELL order, each
+// entry's column offset (column - row) and FP64 value bits.  Rows with equal
+// keys are interchangeable for the recursion: the step kernel then computes
+// their neighbours from a shared table.  Keys are hashed here; equality is
+// confirmed entry by entry afterwards, so a hash collision only costs the
+// class form, never a wrong product.
+__device__ __forceinline__ uint64_t cls_mix(uint64_t x) {
+  x ^= x >> 31;
+  x *= 0x7fb5d329728ea185ull;
+  x ^= x >> 27;
+  x *= 0x81dadef4bc2dd44dull;
+  x ^= x >> 33;
+  return x;
+}
+
+__global__ void class_hash_kernel(int32_t n, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
+                                  const double* __restrict__ v64, int cplx, uint64_t* __restrict__ hash) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t s = i >> 5, l = i & 31;
+  const int64_t base = soff[s];
+  const int32_t w = (soff[s + 1] - soff[s]) >> 5;
+  uint64_t h = 0x9e3779b97f4a7c15ull;
+  int32_t cnt = 0;
+  for (int32_t k = 0; k < w; ++k) {
+    const int64_t o = base + (int64_t)k * 32 + l;
+    const int32_t c = ecol[o];
+    if (c == i) continue;                                  // padding
+    ++cnt;
+    h = cls_mix(h ^ (uint64_t)(uint32_t)(c - i));
+    h = cls_mix(h ^ (uint64_t)__double_as_longlong(cplx ? v64[2 * o] : v64[o]));
+    if (cplx) h = cls_mix(h ^ (uint64_t)__double_as_longlong(v64[2 * o + 1]));
+  }
+  h = cls_mix(h ^ (uint64_t)cnt);
+  hash[i] = h ? h : 1ull;                                  // 0 marks an empty table slot
+}
+
+// Open-addressing insert of every row's key (linear probing, at most cap
+// probes); lanes of a warp with equal keys insert once.  rep[slot] = the
+// smallest row of the key.
+__global__ void class_insert_kernel(int32_t n, const uint64_t* __restrict__ hash,
+                                    unsigned long long* __restrict__ keys, int32_t* __restrict__ rep, int32_t cap,
+                                    int* __restrict__ overflow) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = i < n;
+  const unsigned long long key = act ? (unsigned long long)hash[i] : 0ull;
+  const unsigned m = __match_any_sync(0xffffffffu, key);
+  if (!act || (threadIdx.x & 31) != __ffs(m) - 1) return;
+  uint32_t slot = (uint32_t)(key ^ (key >> 32)) & (uint32_t)(cap - 1);
+  for (int32_t probe = 0; probe < cap; ++probe) {
+    const unsigned long long prev = atomicCAS(&keys[slot], 0ull, key);
+    if (prev == 0ull || prev == key) {
+      atomicMin(&rep[slot], i);
+      return;
+    }
+    slot = (slot + 1) & (uint32_t)(cap - 1);
+  }
+  atomicOr(overflow, 1);
+}
+
+__global__ void class_assign_kernel(int32_t n, const uint64_t* __restrict__ hash,
+                                    const unsigned long long* __restrict__ keys, const int32_t* __restrict__ slot_id,
+                                    int32_t cap, uint8_t* __restrict__ cls, int* __restrict__ bad) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long key = hash[i];
+  uint32_t slot = (uint32_t)(key ^ (key >> 32)) & (uint32_t)(cap - 1);
+  for (int32_t probe = 0; probe < cap; ++probe) {
+    if (keys[slot] == key) {
+      cls[i] = (uint8_t)slot_id[slot];
+      return;
+    }
+    slot = (slot + 1) & (uint32_t)(cap - 1);
+  }
+  atomicOr(bad, 1);
+}
+
+// Every row against its class's representative: same entry count, and in ELL
+// order the same column offsets and bit-identical FP64 values.
+__global__ void class_verify_kernel(int32_t n, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
+                                    const double* __restrict__ v64, int cplx, const uint8_t* __restrict__ cls,
+                                    const int32_t* __restrict__ rep_of, int* __restrict__ bad) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t j = rep_of[cls[i]];
+  const int32_t si = i >> 5, li = i & 31, sj = j >> 5, lj = j & 31;
+  const int32_t wi = (soff[si + 1] - soff[si]) >> 5, wj = (soff[sj + 1] - soff[sj]) >> 5;
+  int32_t ki = 0, kj = 0;
+  const int vs = cplx ? 2 : 1;
+  while (true) {
+    while (ki < wi && ecol[soff[si] + (int64_t)ki * 32 + li] == i) ++ki;
+    while (kj < wj && ecol[soff[sj] + (int64_t)kj * 32 + lj] == j) ++kj;
+    if (ki >= wi || kj >= wj) break;
+    const int64_t oi = soff[si] + (int64_t)ki * 32 + li, oj = soff[sj] + (int64_t)kj * 32 + lj;
+    bool same = (ecol[oi] - i) == (ecol[oj] - j);
+    for (int q = 0; q < vs; ++q)
+      same = same && __double_as_longlong(v64[vs * oi + q]) == __double_as_longlong(v64[vs * oj + q]);
+    if (!same) {
+      atomicOr(bad, 1);
+      return;
+    }
+    ++ki;
+    ++kj;
+  }
+  if (ki < wi || kj < wj) atomicOr(bad, 1);                // different entry counts
+}
+
+// The class table from the representative rows: offsets, counts and the values
+// in every precision (FP32 = the ELL's rounding, double-float = hi, lo as the
+// ELL's double-float copy), unused tail entries zero.
+__global__ void class_table_kernel(int32_t n_cls, int32_t W, const int32_t* __restrict__ rep_of,
+                                   const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
+                                   const double* __restrict__ v64, int cplx, int32_t* __restrict__ cnt,
+                                   int32_t* __restrict__ off, double* __restrict__ t64, float* __restrict__ t32,
+                                   float* __restrict__ tdd) {
+  const int32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cls) return;
+  const int32_t j = rep_of[c], s = j >> 5, l = j & 31;
+  const int32_t w = (soff[s + 1] - soff[s]) >> 5;
+  const int vs = cplx ? 2 : 1;
+  int32_t k = 0;
+  for (int32_t e = 0; e < w; ++e) {
+    const int64_t o = soff[s] + (int64_t)e * 32 + l;
+    if (ecol[o] == j) continue;
+    const int64_t t = (int64_t)c * W + k;
+    off[t] = ecol[o] - j;
+    for (int q = 0; q < vs; ++q) {
+      const double x = v64[vs * o + q];
+      const float h = __double2float_rn(x);
+      t64[vs * t + q] = x;
+      t32[vs * t + q] = h;
+      tdd[2 * (vs * t + q)] = h;
+      tdd[2 * (vs * t + q) + 1] = __double2float_rn(x - (double)h);
+    }
+    ++k;
+  }
+  cnt[c] = k;
+  for (int32_t e = k; e < W; ++e) {
+    const int64_t t = (int64_t)c * W + e;
+    off[t] = 0;
+    for (int q = 0; q < vs; ++q) {
+      t64[vs * t + q] = 0.0;
+      t32[vs * t + q] = 0.f;
+      tdd[2 * (vs * t + q)] = 0.f;
+      tdd[2 * (vs * t + q) + 1] = 0.f;
+    }
+  }
+}
+
+int ensure_classes(tbk_sparse_s* A, cudaStream_t st) {
+  TBK_TRY(ensure_ell(A, st));
+  EllDev& E = A->ell;
+  if (E.cls_state != 0) return TBK_OK;
+  E.cls_state = -1;
+  if (const char* e = getenv("TBK_NO_CLASSES"))           // A/B override: always gather through the ELL
+    if (atoi(e) != 0) return TBK_OK;
+  const int32_t n = E.n_rows;
+  const int32_t W = E.max_width;
+  if (n < 1 || !E.val64.p || !E.col.p) return TBK_OK;
+  if (W > kMaxClassEntries) return TBK_OK;
+  constexpr int32_t cap = 1024;                            // table slots (power of two, > kMaxClasses)
+  DevBuf hash, keys, rep, flags, slot_id, rep_of, cls;
+  TBK_TRY(hash.alloc(sizeof(uint64_t) * n));
+  TBK_TRY(keys.alloc(sizeof(unsigned long long) * cap));
+  TBK_TRY(rep.alloc(sizeof(int32_t) * cap));
+  TBK_TRY(flags.alloc(2 * sizeof(int)));
+  TBK_CUDA(cudaMemsetAsync(keys.p, 0, keys.bytes, st));
+  TBK_CUDA(cudaMemsetAsync(rep.p, 0x7f, rep.bytes, st));
+  TBK_CUDA(cudaMemsetAsync(flags.p, 0, flags.bytes, st));
+  const int T = 256;
+  const unsigned g = (unsigned)((n + T - 1) / T);
+  const int32_t* soff = E.slice_off.as<int32_t>();
+  const int32_t* ecol = E.col.as<int32_t>();
+  const double* v64 = E.val64.as<double>();
+  class_hash_kernel<<<g, T, 0, st>>>(n, soff, ecol, v64, E.cplx, hash.as<uint64_t>());
+  TBK_CHECK_LAUNCH();
+  class_insert_kernel<<<g, T, 0, st>>>(n, hash.as<uint64_t>(), keys.as<unsigned long long>(), rep.as<int32_t>(), cap,
+                                       flags.as<int>());
+  TBK_CHECK_LAUNCH();
+  std::vector<unsigned long long> hk(cap);
+  std::vector<int32_t> hr(cap);
+  int hf[2] = {0, 0};
+  TBK_CUDA(cudaMemcpyAsync(hk.data(), keys.p, keys.bytes, cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaMemcpyAsync(hr.data(), rep.p, rep.bytes, cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaMemcpyAsync(hf, flags.p, sizeof(hf), cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  if (hf[0]) return TBK_OK;                                // more keys than slots
+  // class ids in slot order (deterministic: the slots depend on the keys only)
+  std::vector<int32_t> sid(cap, -1), rof;
+  for (int32_t q = 0; q < cap; ++q)
+    if (hk[q]) {
+      sid[q] = (int32_t)rof.size();
+      rof.push_back(hr[q]);
+    }
+  const int32_t C = (int32_t)rof.size();
+  if (C < 1 || C > kMaxClasses || (int64_t)C * std::max(W, 1) > kMaxClassEntries) return TBK_OK;
+  TBK_TRY(slot_id.alloc(sizeof(int32_t) * cap));
+  TBK_TRY(rep_of.alloc(sizeof(int32_t) * C));
+  TBK_TRY(cls.alloc((size_t)E.n_slices * 32));
+  TBK_CUDA(cudaMemcpyAsync(slot_id.p, sid.data(), sizeof(int32_t) * cap, cudaMemcpyHostToDevice, st));
+  TBK_CUDA(cudaMemcpyAsync(rep_of.p, rof.data(), sizeof(int32_t) * C, cudaMemcpyHostToDevice, st));
+  TBK_CUDA(cudaMemsetAsync(cls.p, 0, cls.bytes, st));
+  class_assign_kernel<<<g, T, 0, st>>>(n, hash.as<uint64_t>(), keys.as<unsigned long long>(), slot_id.as<int32_t>(),
+                                       cap, cls.as<uint8_t>(), flags.as<int>() + 1);
+  TBK_CHECK_LAUNCH();
+  class_verify_kernel<<<g, T, 0, st>>>(n, soff, ecol, v64, E.cplx, cls.as<uint8_t>(), rep_of.as<int32_t>(),
+                                       flags.as<int>() + 1);
+  TBK_CHECK_LAUNCH();
+  const int32_t Wt = std::max(W, 1);
+  const size_t vs = E.cplx ? 2 : 1;
+  DevBuf cnt, off, t64, t32, tdd;
+  TBK_TRY(cnt.alloc(sizeof(int32_t) * C));
+  TBK_TRY(off.alloc(sizeof(int32_t) * C * Wt));
+  TBK_TRY(t64.alloc(sizeof(double) * vs * C * Wt));
+  TBK_TRY(t32.alloc(sizeof(float) * vs * C * Wt));
+  TBK_TRY(tdd.alloc(2 * sizeof(float) * vs * C * Wt));
+  class_table_kernel<<<(C + 63) / 64, 64, 0, st>>>(C, Wt, rep_of.as<int32_t>(), soff, ecol, v64, E.cplx,
+                                                   cnt.as<int32_t>(), off.as<int32_t>(), t64.as<double>(),
+                                                   t32.as<float>(), tdd.as<float>());
+  TBK_CHECK_LAUNCH();
+  TBK_CUDA(cudaMemcpyAsync(hf, flags.p, sizeof(hf), cudaMemcpyDeviceToHost, st));
+  TBK_CUDA(cudaStreamSynchronize(st));
+  if (hf[1]) return TBK_OK;                                // a row differs from its class (hash collision)
+  E.n_cls = C;
+  E.cls_w = Wt;
+  E.cls = std::move(cls);
+  E.cls_cnt = std::move(cnt);
+  E.cls_off = std::move(off);
+  E.cls_v64 = std::move(t64);
+  E.cls_v32 = std::move(t32);
+  E.cls_vdd = std::move(tdd);
+  E.cls_state = 1;
+  return TBK_OK;
+}
+
 }  // namespace tbk
 
 using namespace tbk;
@@ -878,6 +1115,13 @@ int tbk_sparse_from_csc(tbk_sparse* out, int32_t rows, int32_t cols, int64_t nnz
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) { delete A; return fail(TBK_ERR_CUDA, "tbk_sparse_from_csc: %s", cudaGetErrorString(e)); }
   *out = A;
+  return TBK_OK;
+}
+
+int tbk_sparse_row_classes(tbk_sparse A, int32_t* n_classes, void* stream) {
+  if (!A || !n_classes) return fail(TBK_ERR_INVALID, "tbk_sparse_row_classes: null argument");
+  TBK_TRY(ensure_classes(A, as_stream(stream)));
+  *n_classes = A->ell.cls_state == 1 ? A->ell.n_cls : 0;
   return TBK_OK;
 }
 

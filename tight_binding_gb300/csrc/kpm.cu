@@ -206,14 +206,34 @@ const void* ell_diag(const EllDev& E, int prec) {
   return prec == TBK_PREC_MIXED ? E.diag32.p : prec == TBK_PREC_DD ? E.diagdd.p : E.diag64.p;
 }
 
+ClassTab class_tab(const EllDev& E, int prec) {
+  ClassTab t;
+  if (E.cls_state != 1) return t;
+  t.cls = E.cls.as<uint8_t>();
+  t.cnt = E.cls_cnt.as<int32_t>();
+  t.off = E.cls_off.as<int32_t>();
+  t.val = prec == TBK_PREC_MIXED ? E.cls_v32.p : prec == TBK_PREC_DD ? E.cls_vdd.p : E.cls_v64.p;
+  t.n_cls = E.n_cls;
+  t.w = E.cls_w;
+  return t;
+}
+
+size_t class_smem(const EllDev& E, int prec) {
+  if (E.cls_state != 1) return 0;
+  const size_t ne = (size_t)E.n_cls * E.cls_w;
+  const size_t fb = prec == TBK_PREC_MIXED ? 4 : 8;         // float, double, double-float pair
+  return ne * fb * (E.cplx ? 2 : 1) + ne * 4 + (size_t)E.n_cls * 4;
+}
+
 int step_config(tbk_sparse_s* A, int Rc, int prec, int* grid, int* n_tiles, cudaStream_t st) {
   TBK_TRY(ensure_ell(A, st));
   if (prec == TBK_PREC_DD) TBK_TRY(ensure_ell_dd(A, st));
+  TBK_TRY(ensure_classes(A, st));
   const int rpt = rows_per_tile(prec, Rc);
   *n_tiles = (A->rows + rpt - 1) / rpt;
-  int occ = 1;
   const bool cplx = A->ell.cplx != 0;
-  occ = occupancy_prec(prec, cplx, Rc);
+  const int occ = A->ell.cls_state == 1 ? occupancy_cls_prec(prec, cplx, Rc, class_smem(A->ell, prec))
+                                        : occupancy_prec(prec, cplx, Rc);
   *grid = std::max(1, std::min(*n_tiles, sm_count() * occ));
   return TBK_OK;
 }
@@ -285,7 +305,12 @@ int step_ks(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const voi
   return step_dispatch(A, Rc, prec, first, a, grid, st);
 }
 
-static int step_dispatch(tbk_sparse_s* A, int Rc, int prec, bool first, const StepArgs& a, int grid, cudaStream_t st) {
+static int step_dispatch(tbk_sparse_s* A, int Rc, int prec, bool first, const StepArgs& a0, int grid, cudaStream_t st) {
+  StepArgs a = a0;
+  if (A->ell.cls_state == 1 && a.kst != 2) {                // the class form where it applies
+    a.cls = true;
+    a.ct = class_tab(A->ell, prec);
+  }
   return launch_step_prec(prec, A->ell.cplx != 0, Rc, a, first, false, grid, st);
 }
 
@@ -295,9 +320,26 @@ int launch_step_dd(bool cplx, int R, const StepArgs& a, bool first, bool braket,
 int occupancy_f32(bool cplx, int R);
 int occupancy_f64(bool cplx, int R);
 int occupancy_dd(bool cplx, int R);
+int launch_step_cls_f32(bool cplx, int R, const StepArgs& a, bool first, bool braket, int grid, cudaStream_t st);
+int launch_step_cls_f64(bool cplx, int R, const StepArgs& a, bool first, bool braket, int grid, cudaStream_t st);
+int launch_step_cls_dd(bool cplx, int R, const StepArgs& a, bool first, bool braket, int grid, cudaStream_t st);
+int occupancy_cls_f32(bool cplx, int R, size_t smem);
+int occupancy_cls_f64(bool cplx, int R, size_t smem);
+int occupancy_cls_dd(bool cplx, int R, size_t smem);
+
+int occupancy_cls_prec(int prec, bool cplx, int R, size_t smem) {
+  if (prec == TBK_PREC_FP64) return occupancy_cls_f64(cplx, R, smem);
+  if (prec == TBK_PREC_DD) return occupancy_cls_dd(cplx, R, smem);
+  return occupancy_cls_f32(cplx, R, smem);
+}
 
 int launch_step_prec(int prec, bool cplx, int R, const StepArgs& a, bool first, bool braket, int grid,
                      cudaStream_t st) {
+  if (a.cls) {
+    if (prec == TBK_PREC_FP64) return launch_step_cls_f64(cplx, R, a, first, braket, grid, st);
+    if (prec == TBK_PREC_DD) return launch_step_cls_dd(cplx, R, a, first, braket, grid, st);
+    return launch_step_cls_f32(cplx, R, a, first, braket, grid, st);
+  }
   if (prec == TBK_PREC_FP64) return launch_step_f64(cplx, R, a, first, braket, grid, st);
   if (prec == TBK_PREC_DD) return launch_step_dd(cplx, R, a, first, braket, grid, st);
   return launch_step_f32(cplx, R, a, first, braket, grid, st);
@@ -347,6 +389,7 @@ struct tbk_kpm_s {
   TmaLayout lay_dbl{}, lay_brk{};   // stage layouts: doubling / braket
   int grid_dbl = 0, grid_brk = 0, tiles_tma = 0;
   int grid_max = 0;
+  bool use_cls = false;             // one-pass kernel in the class form (translation-invariant H~)
   int pf_dist = 1;                  // L2 prefetch distance of the one-pass kernel (grid-stride waves)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0, last_bytes = 0.0;
@@ -669,6 +712,10 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
       a.gather = last_dot ? 0 : 1;
       a.reverse = (P->flags & TBK_FLAG_NO_L2_ZIGZAG) ? 0 : (s & 1);
       a.pipe = E.max_width > 4;
+      if (P->use_cls && !tma) {
+        a.cls = true;
+        a.ct = class_tab(E, P->prec);
+      }
       const bool first = s == 0;
       int rc;
       if (tma) {
@@ -755,7 +802,9 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
   // algorithmic DRAM bytes per recursion launch (average over the launches)
   const double vec = (double)P->n * P->Rc * P->csize;
   const double hv = (mixed ? 4.0 : 8.0) * (cplx ? 2.0 : 1.0);
-  const double mat = (double)E.n_entries * (4.0 + hv) + (double)E.n_rows * hv + 4.0 * (E.n_slices + 1);
+  // class form: the row's class byte and its diagonal value (the table is in shared memory)
+  const double mat_ell = (double)E.n_entries * (4.0 + hv) + (double)E.n_rows * hv + 4.0 * (E.n_slices + 1);
+  const double mat = (P->use_cls && !tma) ? (double)E.n_rows * (1.0 + hv) : mat_ell;
   double per_chunk = 0.0;
   int32_t s0 = 0;
   if (doubling && P->fused && !tma) {
@@ -763,7 +812,7 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
     // and v_s are read again from L2 by the second step
     for (; s0 + 1 < n_steps; s0 += 2) {
       const bool dot2 = s0 + 1 == n_steps - 1;
-      per_chunk += (s0 > 0 ? 2 : 1) * vec + vec + (dot2 ? 0.0 : vec) + mat;
+      per_chunk += (s0 > 0 ? 2 : 1) * vec + vec + (dot2 ? 0.0 : vec) + mat_ell;
     }
   }
   for (int32_t s = s0; s < n_steps; ++s) {
@@ -808,7 +857,15 @@ int tbk_kpm_create(tbk_kpm* out, tbk_sparse Ht, int32_t R, int32_t flags) {
   P->n_tiles = (int)((P->n + rpt - 1) / rpt);
   int occ = 1;
   const bool cplx = Ht->ell.cplx != 0;
-  occ = occupancy_prec(prec, cplx, rc);
+  {
+    const int s0 = ensure_classes(Ht, st);
+    if (s0 != TBK_OK) {
+      delete P;
+      return s0;
+    }
+  }
+  P->use_cls = Ht->ell.cls_state == 1;
+  occ = P->use_cls ? occupancy_cls_prec(prec, cplx, rc, class_smem(Ht->ell, prec)) : occupancy_prec(prec, cplx, rc);
   P->grid = std::max(1, std::min(P->n_tiles, sm_count() * occ));
   P->grid_max = P->grid;
   if (const char* e = getenv("TBK_PREFETCH")) P->pf_dist = atoi(e);   // tuning override

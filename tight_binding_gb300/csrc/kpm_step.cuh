@@ -13,6 +13,25 @@ namespace tbk {
 constexpr int kStepThreads = 256;
 constexpr int kStepWarps = kStepThreads / 32;
 
+// Row classes of a translation-invariant matrix (EllDev::cls*): class of each
+// row, and per class its entry count, column offsets (column - row) and values
+// in the recursion's precision, w entries per class.
+struct ClassTab {
+  const uint8_t* cls = nullptr;
+  const int32_t* cnt = nullptr;
+  const int32_t* off = nullptr;
+  const void* val = nullptr;
+  int32_t n_cls = 0, w = 0;
+};
+// shared-memory table of the class form: values, offsets, counts
+template <typename F, bool CPLX_H>
+constexpr int class_value_bytes() { return (CPLX_H ? 2 : 1) * (int)sizeof(F); }
+template <typename F, bool CPLX_H>
+inline size_t class_smem_bytes(const ClassTab& ct) {
+  const size_t ne = (size_t)ct.n_cls * ct.w;
+  return ne * class_value_bytes<F, CPLX_H>() + ne * 4 + (size_t)ct.n_cls * 4;
+}
+
 // One recursion step over all rows, x = v_s, y = v_{s-1} on entry.
 //   FIRST: y = H x                    else: y = 2 H x - y  (v_{s+1} over v_{s-1})
 //   doubling (BRAKET false): part[0] += <x|x>; part[1] += <x|y_in> (= <v_s|v_{s-1}>),
@@ -33,12 +52,17 @@ constexpr int kStepWarps = kStepThreads / 32;
 //   are in flight: 4 dependent memory round trips per 12-neighbour row instead
 //   of 6 (1.8x on the FCC Kubo recursion).  Narrow rows keep the plain loop,
 //   whose extra predicated loads would cost the honeycomb recursion 8%.
-template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET, int KST = 0, bool PIPE = false>
+//   CLS: rows of a translation-invariant matrix come in a few classes (ct);
+//   each neighbour is row + offset from the class table in shared memory and
+//   its value comes from there too, so no column index or value is loaded and
+//   the only index read (the row's class byte) is issued one grid-stride
+//   iteration ahead.  Same entries in the same order as the ELL: the same sums.
+template <typename F, int R, bool CPLX_H, bool FIRST, bool BRAKET, int KST = 0, bool PIPE = false, bool CLS = false>
 __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     int32_t n, int32_t n_tiles, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
     const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
     typename C2<F>::T* y, const typename C2<F>::T* pv, const typename C2<F>::T* __restrict__ bras,
-    double* __restrict__ part, int store, int reverse, int gather, int pf_dist, const KStore ks) {
+    double* __restrict__ part, int store, int reverse, int gather, int pf_dist, const KStore ks, const ClassTab ct) {
   using CT = typename C2<F>::T;
   constexpr int VPL = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
   constexpr int LPR = R / VPL;             // lanes per row
@@ -50,8 +74,42 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sub = lane % LPR;
   Acc m0 = 0, m1 = 0;
+  static_assert(!(CLS && (PIPE || KST == 2)), "class form: no column pipeline, no operator products");
+
+  // class form: the table in shared memory (4-byte words: values, offsets, counts)
+  extern __shared__ __align__(16) unsigned char cls_smem[];
+  const F* s_val = reinterpret_cast<const F*>(cls_smem);
+  const int32_t* s_off = nullptr;
+  const int32_t* s_cnt = nullptr;
+  uint32_t c_next = 0;                     // class of this thread's row in the next iteration
+  if constexpr (CLS) {
+    const int32_t ne = ct.n_cls * ct.w;
+    const int32_t vw = ne * (class_value_bytes<F, CPLX_H>() / 4);
+    uint32_t* sw = reinterpret_cast<uint32_t*>(cls_smem);
+    const uint32_t* gv = static_cast<const uint32_t*>(ct.val);
+    for (int32_t q = threadIdx.x; q < vw; q += blockDim.x) sw[q] = gv[q];
+    for (int32_t q = threadIdx.x; q < ne; q += blockDim.x) sw[vw + q] = (uint32_t)ct.off[q];
+    for (int32_t q = threadIdx.x; q < ct.n_cls; q += blockDim.x) sw[vw + ne + q] = (uint32_t)ct.cnt[q];
+    s_off = reinterpret_cast<const int32_t*>(sw + vw);
+    s_cnt = reinterpret_cast<const int32_t*>(sw + vw + ne);
+    __syncthreads();
+    const int32_t t0 = blockIdx.x;
+    if (t0 < n_tiles) {
+      const int32_t r0 = (reverse ? (n_tiles - 1 - t0) : t0) * ROWS_PER_TILE + warp * RPW + lane / LPR;
+      if (r0 < n) c_next = __ldg(ct.cls + r0);
+    }
+  }
 
   for (int32_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const uint32_t c_cur = c_next;
+    if constexpr (CLS) {
+      const int32_t tn = t + (int32_t)gridDim.x;
+      c_next = 0;
+      if (tn < n_tiles) {
+        const int32_t rn = (reverse ? (n_tiles - 1 - tn) : tn) * ROWS_PER_TILE + warp * RPW + lane / LPR;
+        if (rn < n) c_next = __ldg(ct.cls + rn);
+      }
+    }
     const int32_t tile = reverse ? (n_tiles - 1 - t) : t;
     if (pf_dist > 0 && threadIdx.x == 0) {
       // bring the streams of the tile this CTA reaches pf_dist iterations later
@@ -92,7 +150,26 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
 #pragma unroll
       for (int q = 0; q < VPL; ++q) { vacc.re[q] = 0; vacc.im[q] = 0; }
     }
-    if (gather) {
+    if (gather && CLS) {
+      HVal<F, CPLX_H>::load(diag, r).template fma<VPL>(xs, acc);
+      const int32_t cnt = s_cnt[c_cur];
+      const int32_t tb = (int32_t)c_cur * ct.w;
+      for (int k = 0; k < cnt; k += 4) {
+        HVal<F, CPLX_H> h[4];
+        LaneV<F, VPL> xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const bool v = k + u < cnt;
+          // rows are verified equal to their class, so r + offset is the
+          // row's column; the clamp only keeps a bad table inside the block
+          const int32_t c = v ? min(max(r + s_off[tb + k + u], 0), n - 1) : r;
+          h[u] = v ? HVal<F, CPLX_H>::load_smem(s_val, tb + k + u) : HVal<F, CPLX_H>::zero();
+          xv[u] = v ? ld_ro<F, VPL>(x + ((int64_t)c * LPR + sub) * VPL) : xs;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
+      }
+    } else if (gather) {
       HVal<F, CPLX_H>::load(diag, r).template fma<VPL>(xs, acc);
       if constexpr (KST == 2) HVal<F, CPLX_H>::load(vdiag, r).template fma<VPL>(xs, vacc);
       const int32_t s = r >> 5, l = r & 31;
@@ -227,11 +304,14 @@ struct StepArgs {
   KStore ks;                   // optional complex64 K-tiled stores (Kubo blocks)
   int kst = 0;                 // 0 none, 1 output into ks.store[0], 2 per-group output / V x
   bool pipe = false;           // ELL wider than 4: pipelined column loads
+  bool cls = false;            // row classes (ct) instead of the ELL's columns and values
+  ClassTab ct;
 };
 
-template <typename F, int R, bool CPLX_H>
+template <typename F, int R, bool CPLX_H, bool CLS>
 inline int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, cudaStream_t st) {
   using CT = typename C2<F>::T;
+  const size_t smem = CLS ? class_smem_bytes<F, CPLX_H>(a.ct) : 0;
   auto x = static_cast<const CT*>(a.x);
   auto y = static_cast<CT*>(a.y);
   auto pv = static_cast<const CT*>(a.pv ? a.pv : a.y);
@@ -240,12 +320,18 @@ inline int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
   auto dg = static_cast<const F*>(a.diag);
 #define TBK_STEP(FI, BR, KS)                                                                          \
   do {                                                                                                \
-    if (a.pipe)                                                                                       \
+    if constexpr (CLS)                                                                                \
+      kpm_step_kernel<F, R, CPLX_H, FI, BR, KS, false, true><<<grid, kStepThreads, smem, st>>>(       \
+          a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.ks, \
+          a.ct);                                                                                      \
+    else if (a.pipe)                                                                                  \
       kpm_step_kernel<F, R, CPLX_H, FI, BR, KS, true><<<grid, kStepThreads, 0, st>>>(                 \
-          a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.ks); \
+          a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.ks, \
+          a.ct);                                                                                      \
     else                                                                                              \
       kpm_step_kernel<F, R, CPLX_H, FI, BR, KS, false><<<grid, kStepThreads, 0, st>>>(                \
-          a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.ks); \
+          a.n, a.n_tiles, a.soff, a.ecol, ev, dg, x, y, pv, b, a.part, a.store, a.reverse, a.gather, a.pf_dist, a.ks, \
+          a.ct);                                                                                      \
   } while (0)
   if (a.kst != 0) {
     if (braket) return fail(TBK_ERR_UNSUPPORTED, "K-tiled store with a braket step");
@@ -255,7 +341,10 @@ inline int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
     if (a.kst == 3) {
       if (first) return fail(TBK_ERR_UNSUPPORTED, "Clenshaw term on a first step");
       TBK_STEP(false, false, 3);
-    } else if (a.kst == 2) { if (first) TBK_STEP(true, false, 2); else TBK_STEP(false, false, 2); }
+    } else if (a.kst == 2) {
+      if constexpr (CLS) return fail(TBK_ERR_UNSUPPORTED, "operator products in the class form");
+      else { if (first) TBK_STEP(true, false, 2); else TBK_STEP(false, false, 2); }
+    }
     else { if (first) TBK_STEP(true, false, 1); else TBK_STEP(false, false, 1); }
   } else if (first) { if (braket) TBK_STEP(true, true, 0); else TBK_STEP(true, false, 0); }
   else { if (braket) TBK_STEP(false, true, 0); else TBK_STEP(false, false, 0); }
@@ -264,33 +353,51 @@ inline int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
   return TBK_OK;
 }
 
-template <typename F, bool CPLX_H>
+template <typename F, bool CPLX_H, bool CLS = false>
 inline int launch_step(int R, const StepArgs& a, bool first, bool braket, int grid, cudaStream_t st) {
   switch (R) {
-    case 1: return launch_step_r<F, 1, CPLX_H>(a, first, braket, grid, st);
-    case 2: return launch_step_r<F, 2, CPLX_H>(a, first, braket, grid, st);
-    case 4: return launch_step_r<F, 4, CPLX_H>(a, first, braket, grid, st);
-    case 8: return launch_step_r<F, 8, CPLX_H>(a, first, braket, grid, st);
-    case 16: return launch_step_r<F, 16, CPLX_H>(a, first, braket, grid, st);
-    case 32: return launch_step_r<F, 32, CPLX_H>(a, first, braket, grid, st);
+    case 1: return launch_step_r<F, 1, CPLX_H, CLS>(a, first, braket, grid, st);
+    case 2: return launch_step_r<F, 2, CPLX_H, CLS>(a, first, braket, grid, st);
+    case 4: return launch_step_r<F, 4, CPLX_H, CLS>(a, first, braket, grid, st);
+    case 8: return launch_step_r<F, 8, CPLX_H, CLS>(a, first, braket, grid, st);
+    case 16: return launch_step_r<F, 16, CPLX_H, CLS>(a, first, braket, grid, st);
+    case 32: return launch_step_r<F, 32, CPLX_H, CLS>(a, first, braket, grid, st);
     case 64:
-      if constexpr (sizeof(F) == 4) return launch_step_r<F, 64, CPLX_H>(a, first, braket, grid, st);
+      if constexpr (sizeof(F) == 4) return launch_step_r<F, 64, CPLX_H, CLS>(a, first, braket, grid, st);
       break;
   }
   return fail(TBK_ERR_UNSUPPORTED, "chunk width %d not instantiated", R);
 }
 
 
-template <typename F, bool CPLX_H, int R>
-inline int occupancy_blocks() {
+template <typename F, bool CPLX_H, int R, bool CLS = false>
+inline int occupancy_blocks(size_t smem = 0) {
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kpm_step_kernel<F, R, CPLX_H, false, false, 0, false>, kStepThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kpm_step_kernel<F, R, CPLX_H, false, false, 0, false, CLS>,
+                                                kStepThreads, smem);
   return nb > 0 ? nb : 1;
 }
 
-// per-precision entry points (TBK_PREC_*)
+template <typename F, bool CLS>
+inline int occupancy_r(bool cplx, int R, size_t smem) {
+  switch (R) {
+    case 1: return cplx ? occupancy_blocks<F, true, 1, CLS>(smem) : occupancy_blocks<F, false, 1, CLS>(smem);
+    case 2: return cplx ? occupancy_blocks<F, true, 2, CLS>(smem) : occupancy_blocks<F, false, 2, CLS>(smem);
+    case 4: return cplx ? occupancy_blocks<F, true, 4, CLS>(smem) : occupancy_blocks<F, false, 4, CLS>(smem);
+    case 8: return cplx ? occupancy_blocks<F, true, 8, CLS>(smem) : occupancy_blocks<F, false, 8, CLS>(smem);
+    case 16: return cplx ? occupancy_blocks<F, true, 16, CLS>(smem) : occupancy_blocks<F, false, 16, CLS>(smem);
+    default: return cplx ? occupancy_blocks<F, true, 32, CLS>(smem) : occupancy_blocks<F, false, 32, CLS>(smem);
+  }
+}
+
+// per-precision entry points (TBK_PREC_*); a.cls selects the class form
 int launch_step_prec(int prec, bool cplx, int R, const StepArgs& a, bool first, bool braket, int grid,
                      cudaStream_t st);
 int occupancy_prec(int prec, bool cplx, int R);
+// CTAs per SM of the class-form kernel with its shared-memory table
+int occupancy_cls_prec(int prec, bool cplx, int R, size_t smem);
+// the class table of a matrix in a precision (ct.n_cls == 0: no class form)
+ClassTab class_tab(const EllDev& E, int prec);
+size_t class_smem(const EllDev& E, int prec);
 
 }  // namespace tbk

@@ -99,7 +99,24 @@ struct EllDev {
   DevBuf diag32;      // float / float2 [n_rows]
   DevBuf valdd;       // double-float (hi, lo) pairs, real or complex [n_entries] (on demand)
   DevBuf diagdd;      // [n_rows]
+  // Row classes (ensure_classes): when every row's off-diagonal entries form
+  // one of at most kMaxClasses lists of (column - row, value) — the case of a
+  // lattice Hamiltonian without vacancies whose hoppings do not vary from cell
+  // to cell — the recursion computes each neighbour as row + offset from the
+  // row's class instead of loading its column index and value.  Exact: every
+  // row is compared entry by entry with its class's representative row.
+  int32_t cls_state = 0;   // 0 not examined, 1 classes ready, -1 not applicable
+  int32_t n_cls = 0;       // number of classes
+  int32_t cls_w = 0;       // table row length (max entries of a class; = max_width)
+  DevBuf cls;              // uint8 [n_slices * 32]: class of each row (0 for the tail)
+  DevBuf cls_cnt;          // int32 [n_cls]: entries of each class
+  DevBuf cls_off;          // int32 [n_cls * cls_w]: column - row, ELL order
+  DevBuf cls_v64;          // double / double2 [n_cls * cls_w]
+  DevBuf cls_v32;          // float / float2
+  DevBuf cls_vdd;          // double-float pairs (real: float2, complex: float4)
 };
+constexpr int32_t kMaxClasses = 255;
+constexpr int32_t kMaxClassEntries = 1024;   // n_cls * cls_w (shared-memory table of the step kernel)
 
 }  // namespace tbk
 
@@ -120,6 +137,7 @@ namespace tbk {
 // builder.cu
 int ensure_ell(tbk_sparse_s* A, cudaStream_t st);
 int ensure_ell_dd(tbk_sparse_s* A, cudaStream_t st);   // double-float copy of the FP64 values
+int ensure_classes(tbk_sparse_s* A, cudaStream_t st);  // row classes of the ELL (cls_state 1 or -1)
 int exclusive_scan_i32(const int32_t* in, int32_t* out, int64_t n, cudaStream_t st, int32_t* total_host);
 int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t st, int64_t* total_host);
 int sm_count();

@@ -72,6 +72,12 @@ class SparseMatrix:
     def rows(self) -> int:
         return self.shape[0]
 
+    def row_classes(self) -> int:
+        """Number of row classes the recursion uses for this matrix (0: ELL form)."""
+        n = C.c_int32()
+        check(lib().tbk_sparse_row_classes(self._h, C.byref(n), None))
+        return n.value
+
     def nonZeros(self) -> int:  # Eigen spelling
         return self.nnz
 
