@@ -326,8 +326,10 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   double rec_bytes = 0.0;
   const double vecb = (double)blk * csz, stb = (double)blk * 8.0;
   const int vsz = prec == TBK_PREC_MIXED ? 4 : 8;
+  // class form (row classes): the row's class byte and diagonal; the table is in shared memory
   auto ell_bytes = [&](tbk_sparse_s* A, bool cols) {
     const double hv = (double)vsz * (A->ell.cplx ? 2 : 1);
+    if (cols && A->ell.cls_state == 1) return (double)A->rows * (1.0 + hv);
     return (double)A->ell.n_entries * ((cols ? 4.0 : 0.0) + hv) + (double)A->rows * hv;
   };
   auto apply = [&](tbk_sparse_s* A, const void* x, void* y) -> int {   // y = A x
