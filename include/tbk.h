@@ -66,12 +66,15 @@ enum {
   TBK_FLAG_NO_GRAPH = 1 << 9,     /* never replay the recursion as a CUDA graph
                                      (small single-chunk plans capture their
                                      launch sequence on the second identical run) */
-  TBK_FLAG_PERSISTENT = 1 << 10   /* small single-chunk plans: the whole recursion
+  TBK_FLAG_PERSISTENT = 1 << 10,  /* small single-chunk plans: the whole recursion
                                      in one launch, one thread-block cluster per
                                      random vector holding its rows and H~ in
                                      shared memory (opt-in: on the 4,096-site
                                      case it matches graph replay in complex64
                                      and is slower in FP64)                     */
+  TBK_FLAG_NO_CACHE = 1 << 11     /* tbk_cheb_braket_*: build and free the matrix
+                                     and plan in this call instead of reusing
+                                     the cached ones                           */
 };
 
 /* =========================================================================
@@ -280,7 +283,14 @@ int tbk_moments_load(const char* path, tbk_moments_header* header, double* data,
  * compressed), bras/kets N x R column-major complex128; mu_out[k] =
  * Re tr(bras^dagger T_k(M) kets), k < n.  n < 2 -> TBK_ERR_INVALID (the
  * reference returns an empty vector).  flags: TBK_PREC_* | TBK_FLAG_DOUBLING
- * (doubling needs bras == kets, same pointer). */
+ * (doubling needs bras == kets, same pointer) | TBK_FLAG_NO_CACHE.
+ * Every call uploads the CSC arrays and compares them on the device with the
+ * previous call's; an identical matrix reuses its device form (ELL, row
+ * classes) and the recursion plan of the same R and flags (work blocks, the
+ * captured launch graph), which the reference rebuilds per call
+ * (TB/numerics_cuda.cu:199-222).  The cache keeps that device memory after the
+ * call (about the matrix plus three vector blocks); tbk_cheb_braket_release
+ * frees it.  Calls are serialised by a lock. */
 int tbk_cheb_braket_real(int32_t n_rows, int64_t nnz, const int32_t* col_ptr,
                          const int32_t* row_idx, const double* values, int32_t n,
                          const double* bras, const double* kets, int32_t R, int32_t flags,
@@ -290,6 +300,9 @@ int tbk_cheb_braket_complex(int32_t n_rows, int64_t nnz, const int32_t* col_ptr,
                             const int32_t* row_idx, const double* values, int32_t n,
                             const double* bras, const double* kets, int32_t R,
                             int32_t flags, double* mu_out);
+/* Frees the matrix and plans cached by tbk_cheb_braket_* (no counterpart in
+ * the reference, which keeps nothing between calls). */
+void tbk_cheb_braket_release(void);
 
 /* Resident solver: H~ and the recursion state stay on the device between runs.
  * Replaces the per-call upload/alloc of TB/numerics_cuda.cu:199-222. */

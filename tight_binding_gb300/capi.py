@@ -33,6 +33,7 @@ FLAG_STAGED = 1 << 7
 FLAG_TWO_STEP = 1 << 8
 FLAG_NO_GRAPH = 1 << 9
 FLAG_PERSISTENT = 1 << 10
+FLAG_NO_CACHE = 1 << 11
 
 BUILD_SPARSE = 0
 BUILD_PERIODIC_BARE = 1
@@ -132,6 +133,7 @@ SIGNATURES = {
     "tbk_cheb_evolution_terms": (C.c_int, [C.c_double, C.c_double, C.c_double, _pi32]),
     "tbk_cheb_braket_real": (C.c_int, [_i32, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _i32, _i32, _vp]),
     "tbk_cheb_braket_complex": (C.c_int, [_i32, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _i32, _i32, _vp]),
+    "tbk_cheb_braket_release": (None, []),
     "tbk_kpm_create": (C.c_int, [C.POINTER(_vp), _vp, _i32, _i32]),
     "tbk_kpm_run": (C.c_int, [_vp, _i32, _vp, _vp, _vp, _vp]),
     "tbk_kpm_run_random": (C.c_int, [_vp, _i32, _u64, _vp, _vp]),

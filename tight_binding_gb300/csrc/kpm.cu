@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "host_model.h"
@@ -997,6 +998,128 @@ int tbk_kpm_last_timing(tbk_kpm P, double* ms, int32_t* launches, double* bytes)
   return TBK_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Drop-in plan cache.  The reference's callers (GreenFunctionImag,
+// TB/lattice.h:605-615) call Cheb_first_kind_seq_braket again and again with
+// the same rescaled matrix; every call still uploads the CSC arrays (the
+// reference's contract: host inputs), and a device comparison against the
+// arrays of the previous call decides whether the matrix, its ELL and row
+// classes and the recursion plans (work blocks, captured graphs) can be
+// reused.  A different matrix replaces the cached one; tbk_cheb_braket_release
+// frees everything; TBK_FLAG_NO_CACHE builds and frees per call.
+struct DropinCache {
+  std::mutex mu;
+  tbk_sparse H = nullptr;
+  int32_t rows = -1, cplx = -1;
+  int64_t nnz = -1;
+  DevBuf stage, flag;
+  struct Plan {
+    int32_t R, flags;
+    tbk_kpm P;
+  };
+  std::vector<Plan> plans;
+  void drop_plans() {
+    for (auto& q : plans) tbk_kpm_destroy(q.P);
+    plans.clear();
+  }
+  void drop() {
+    drop_plans();
+    if (H) tbk_sparse_destroy(H);
+    H = nullptr;
+    rows = cplx = -1;
+    nnz = -1;
+    stage.release();
+    flag.release();
+  }
+};
+DropinCache g_dropin;
+constexpr size_t kDropinPlans = 4;
+
+__global__ void words_differ_kernel(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, int64_t nw,
+                                    int* __restrict__ flag) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nw; q += (int64_t)gridDim.x * blockDim.x)
+    if (a[q] != b[q]) {
+      atomicOr(flag, 1);
+      return;
+    }
+}
+
+int words_differ(const void* a, const void* b, size_t bytes, int* flag, cudaStream_t st) {
+  const int64_t nw = (int64_t)(bytes / 4);
+  if (nw == 0) return TBK_OK;
+  const unsigned g = (unsigned)std::min<int64_t>((nw + 255) / 256, 4096);
+  words_differ_kernel<<<g, 256, 0, st>>>(static_cast<const uint32_t*>(a), static_cast<const uint32_t*>(b), nw, flag);
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
+}
+
+size_t align16(size_t b) { return (b + 15) & ~size_t(15); }
+
+int cheb_braket_cached(int32_t n_rows, int64_t nnz, const int32_t* cp, const int32_t* ri, const double* v, int cplx,
+                       int32_t n, const double* bras, const double* kets, int32_t R, int32_t flags,
+                       double* mu_out) {
+  DropinCache& C = g_dropin;
+  std::lock_guard<std::mutex> lock(C.mu);
+  cudaStream_t st = nullptr;                               // synchronous, as the reference
+  const size_t bcp = sizeof(int32_t) * ((size_t)n_rows + 1), bri = sizeof(int32_t) * (size_t)nnz;
+  const size_t bv = sizeof(double) * (cplx ? 2 : 1) * (size_t)nnz;
+  const size_t o_ri = align16(bcp), o_v = o_ri + align16(bri), need = o_v + align16(bv);
+  if (C.stage.bytes < need) TBK_TRY(C.stage.alloc(need));
+  if (!C.flag.p) TBK_TRY(C.flag.alloc(sizeof(int)));
+  char* sb = C.stage.as<char>();
+  TBK_CUDA(cudaMemcpyAsync(sb, cp, bcp, cudaMemcpyHostToDevice, st));
+  if (nnz) {
+    TBK_CUDA(cudaMemcpyAsync(sb + o_ri, ri, bri, cudaMemcpyHostToDevice, st));
+    TBK_CUDA(cudaMemcpyAsync(sb + o_v, v, bv, cudaMemcpyHostToDevice, st));
+  }
+  bool same = C.H && C.rows == n_rows && C.nnz == nnz && C.cplx == cplx;
+  if (same) {
+    TBK_CUDA(cudaMemsetAsync(C.flag.p, 0, sizeof(int), st));
+    TBK_TRY(words_differ(sb, C.H->col_ptr.p, bcp, C.flag.as<int>(), st));
+    TBK_TRY(words_differ(sb + o_ri, C.H->row_idx.p, bri, C.flag.as<int>(), st));
+    TBK_TRY(words_differ(sb + o_v, C.H->values.p, bv, C.flag.as<int>(), st));
+    int h = 1;
+    TBK_CUDA(cudaMemcpyAsync(&h, C.flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TBK_CUDA(cudaStreamSynchronize(st));
+    same = h == 0;
+  }
+  if (!same) {
+    C.drop_plans();
+    if (C.H) tbk_sparse_destroy(C.H);
+    C.H = nullptr;
+    C.rows = C.cplx = -1;
+    C.nnz = -1;
+    tbk_sparse H = nullptr;
+    TBK_TRY(tbk_sparse_from_csc(&H, n_rows, n_rows, nnz, reinterpret_cast<const int32_t*>(sb),
+                                reinterpret_cast<const int32_t*>(sb + o_ri), reinterpret_cast<const double*>(sb + o_v),
+                                cplx, 1, nullptr));
+    C.H = H;
+    C.rows = n_rows;
+    C.nnz = nnz;
+    C.cplx = cplx;
+  }
+  const int32_t pf = flags & ~TBK_FLAG_DEVICE_PTRS;
+  tbk_kpm P = nullptr;
+  for (auto& q : C.plans)
+    if (q.R == R && q.flags == pf) P = q.P;
+  if (!P) {
+    if (C.plans.size() >= kDropinPlans) {
+      tbk_kpm_destroy(C.plans.front().P);
+      C.plans.erase(C.plans.begin());
+    }
+    TBK_TRY(tbk_kpm_create(&P, C.H, R, pf));
+    C.plans.push_back({R, pf, P});
+  }
+  return tbk_kpm_run(P, n, bras, kets, mu_out, nullptr);
+}
+
+}  // namespace
+
+extern "C" {
+
 static int cheb_braket_common(int32_t n_rows, int64_t nnz, const int32_t* cp, const int32_t* ri,
                               const double* v, int cplx, int32_t n, const double* bras, const double* kets,
                               int32_t R, int32_t flags, double* mu_out) {
@@ -1004,16 +1127,24 @@ static int cheb_braket_common(int32_t n_rows, int64_t nnz, const int32_t* cp, co
     return fail(TBK_ERR_INVALID, "Cheb_first_kind_seq_braket: null argument");
   if (n < 2) return fail(TBK_ERR_INVALID, "n must be greater than or equal to 2");
   if (n_rows < 1 || R < 1) return fail(TBK_ERR_INVALID, "Cheb_first_kind_seq_braket: empty input");
+  if (nnz < 0 || nnz > INT32_MAX) return fail(TBK_ERR_INVALID, "Cheb_first_kind_seq_braket: bad nnz");
   if ((flags & TBK_FLAG_DOUBLING) && bras != kets)
     return fail(TBK_ERR_INVALID, "TBK_FLAG_DOUBLING needs bras == kets");
+  if (!(flags & TBK_FLAG_NO_CACHE))
+    return cheb_braket_cached(n_rows, nnz, cp, ri, v, cplx, n, bras, kets, R, flags & ~TBK_FLAG_NO_CACHE, mu_out);
   tbk_sparse H = nullptr;
   TBK_TRY(tbk_sparse_from_csc(&H, n_rows, n_rows, nnz, cp, ri, v, cplx, 0, nullptr));
   tbk_kpm P = nullptr;
-  int s = tbk_kpm_create(&P, H, R, flags & ~TBK_FLAG_DEVICE_PTRS);
+  int s = tbk_kpm_create(&P, H, R, flags & ~(TBK_FLAG_DEVICE_PTRS | TBK_FLAG_NO_CACHE));
   if (s == TBK_OK) s = tbk_kpm_run(P, n, bras, kets, mu_out, nullptr);
   tbk_kpm_destroy(P);
   tbk_sparse_destroy(H);
   return s;
+}
+
+void tbk_cheb_braket_release(void) {
+  std::lock_guard<std::mutex> lock(g_dropin.mu);
+  g_dropin.drop();
 }
 
 int tbk_cheb_braket_real(int32_t n_rows, int64_t nnz, const int32_t* cp, const int32_t* ri, const double* v,
