@@ -243,7 +243,7 @@ static int step_dispatch(tbk_sparse_s* A, int Rc, int prec, bool first, const St
 
 int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
              int grid, int n_tiles, cudaStream_t st, float2* kstore, int32_t kM, int32_t km, bool store_y,
-             tbk_sparse_s* vop) {
+             tbk_sparse_s* vop, bool dots) {
   StepArgs a;
   a.n = A->rows;
   a.n_tiles = n_tiles;
@@ -276,6 +276,8 @@ int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const vo
     }
   } else if (vop) {
     return fail(TBK_ERR_INVALID, "operator product without a store");
+  } else if (!dots) {
+    a.kst = 4;
   }
   return step_dispatch(A, Rc, prec, first, a, grid, st);
 }

@@ -65,6 +65,57 @@ __device__ __forceinline__ void dd_fma_acc(dd h, dd x, dd& acc) {
   acc.hi = s;
   acc.lo = __fadd_rn(acc.lo, __fadd_rn(t, e));
 }
+// The same accumulation for two values that share the factor h (the real and
+// imaginary parts of one vector element): Blackwell's packed f32x2 arithmetic
+// does both halves in one instruction, each half rounded exactly as the scalar
+// dd_fma_acc rounds it (the product is formed negated, np = (-h) x, so that
+// e = fma(h, x, np) and s = acc - np need no separate negation; rounding is
+// symmetric in sign, so every intermediate equals its scalar counterpart).
+// hh / nhh / hl: (h.hi, h.hi), (-h.hi, -h.hi), (h.lo, h.lo) for a shared
+// factor, or per-half factors for the cross terms of a complex product.
+__device__ __forceinline__ uint64_t f2_pack(float a, float b) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+__device__ __forceinline__ void dd_fma_acc2(uint64_t hh, uint64_t nhh, uint64_t hl, dd xa, dd xb, dd& acca,
+                                            dd& accb) {
+  const uint64_t xh = f2_pack(xa.hi, xb.hi), xl = f2_pack(xa.lo, xb.lo);
+  const uint64_t ah = f2_pack(acca.hi, accb.hi), al = f2_pack(acca.lo, accb.lo);
+  const uint64_t np = f2_mul(nhh, xh);                    // -p
+  uint64_t e = f2_fma(hh, xh, np);                        // exact error of p
+  e = f2_fma(hh, xl, e);
+  e = f2_fma(hl, xh, e);
+  const uint64_t s = f2_sub(ah, np);                      // acc.hi + p
+  const uint64_t bb = f2_sub(s, ah);
+  const uint64_t t = f2_sub(f2_sub(ah, f2_sub(s, bb)), f2_add(np, bb));   // TwoSum error: (ah - (s - bb)) + (p - bb)
+  const uint64_t lo = f2_add(al, f2_add(t, e));
+  f2_unpack(s, acca.hi, accb.hi);
+  f2_unpack(lo, acca.lo, accb.lo);
+}
 __device__ __forceinline__ dd dd_norm(dd a) {            // TwoSum(hi, lo)
   const float s = __fadd_rn(a.hi, a.lo);
   const float bb = __fsub_rn(s, a.hi);
@@ -172,12 +223,14 @@ struct HVal<F, false> {
   __device__ __forceinline__ static HVal zero() { return HVal{F(0)}; }
   template <int VPL>
   __device__ __forceinline__ void fma(const LaneV<F, VPL>& x, LaneV<F, VPL>& acc) const {
+    if constexpr (is_dd<F>) {
+      // real and imaginary parts share v: one packed accumulation per element
+      const uint64_t hh = f2_pack(v.hi, v.hi), nhh = f2_pack(-v.hi, -v.hi), hl = f2_pack(v.lo, v.lo);
 #pragma unroll
-    for (int q = 0; q < VPL; ++q) {
-      if constexpr (is_dd<F>) {
-        dd_fma_acc(v, x.re[q], acc.re[q]);
-        dd_fma_acc(v, x.im[q], acc.im[q]);
-      } else {
+      for (int q = 0; q < VPL; ++q) dd_fma_acc2(hh, nhh, hl, x.re[q], x.im[q], acc.re[q], acc.im[q]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) {
         acc.re[q] = fma_(v, x.re[q], acc.re[q]);
         acc.im[q] = fma_(v, x.im[q], acc.im[q]);
       }
@@ -204,14 +257,19 @@ struct HVal<F, true> {
   __device__ __forceinline__ static HVal zero() { return HVal{F(0), F(0)}; }
   template <int VPL>
   __device__ __forceinline__ void fma(const LaneV<F, VPL>& x, LaneV<F, VPL>& acc) const {
+    if constexpr (is_dd<F>) {
+      // (re, im) += r (x.re, x.im), then (re, im) += (-i x.im, i x.re): the
+      // scalar order of both components, two packed accumulations
+      const uint64_t rh = f2_pack(r.hi, r.hi), nrh = f2_pack(-r.hi, -r.hi), rl = f2_pack(r.lo, r.lo);
+      const uint64_t ih = f2_pack(-i.hi, i.hi), nih = f2_pack(i.hi, -i.hi), il = f2_pack(-i.lo, i.lo);
 #pragma unroll
-    for (int q = 0; q < VPL; ++q) {
-      if constexpr (is_dd<F>) {
-        dd_fma_acc(r, x.re[q], acc.re[q]);
-        dd_fma_acc(-i, x.im[q], acc.re[q]);
-        dd_fma_acc(r, x.im[q], acc.im[q]);
-        dd_fma_acc(i, x.re[q], acc.im[q]);
-      } else {
+      for (int q = 0; q < VPL; ++q) {
+        dd_fma_acc2(rh, nrh, rl, x.re[q], x.im[q], acc.re[q], acc.im[q]);
+        dd_fma_acc2(ih, nih, il, x.im[q], x.re[q], acc.re[q], acc.im[q]);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < VPL; ++q) {
         acc.re[q] = r * x.re[q] + acc.re[q];
         acc.re[q] = -i * x.im[q] + acc.re[q];
         acc.im[q] = r * x.im[q] + acc.im[q];

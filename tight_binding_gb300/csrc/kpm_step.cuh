@@ -47,6 +47,8 @@ inline size_t class_smem_bytes(const ClassTab& ct) {
 //   two sides of a Kubo pair can run as one recursion of twice the width.  A
 //   template parameter because even an untaken runtime branch there costs the
 //   moments recursion ~8% of its bandwidth.
+//   KST = 4: a plain step whose moments nothing reads (the Kubo recursion
+//   ahead of an operator product).  Only KST = 0 forms the moment sums.
 //   PIPE: rows wider than one group of 4 gathers (ELL width > 4, e.g. FCC's
 //   12 neighbours) load the next group's columns while this group's gathers
 //   are in flight: 4 dependent memory round trips per 12-neighbour row instead
@@ -229,8 +231,10 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
         out.im[q] = out.im[q] + (cr * vv.im[q] + ci * vv.re[q]);
       }
     }
-    // moment partial sums (before the store, from registers only)
-    if constexpr (BRAKET) {
+    // moment partial sums (before the store, from registers only); steps that
+    // feed stores, expansions or an operator product need none
+    if constexpr (KST != 0) {
+    } else if constexpr (BRAKET) {
       const LaneV<F, VPL> b = ld_ro<F, VPL>(bras + me * VPL);
 #pragma unroll
       for (int q = 0; q < VPL; ++q) {
@@ -302,7 +306,8 @@ struct StepArgs {
   double* part;
   int store, reverse, gather, pf_dist;
   KStore ks;                   // optional complex64 K-tiled stores (Kubo blocks)
-  int kst = 0;                 // 0 none, 1 output into ks.store[0], 2 per-group output / V x
+  int kst = 0;                 // 0 moments, 1 output into ks.store[0], 2 per-group output / V x,
+                               // 3 Clenshaw term, 4 plain step without moment sums
   bool pipe = false;           // ELL wider than 4: pipelined column loads
   bool cls = false;            // row classes (ct) instead of the ELL's columns and values
   ClassTab ct;
@@ -341,6 +346,8 @@ inline int launch_step_r(const StepArgs& a, bool first, bool braket, int grid, c
     if (a.kst == 3) {
       if (first) return fail(TBK_ERR_UNSUPPORTED, "Clenshaw term on a first step");
       TBK_STEP(false, false, 3);
+    } else if (a.kst == 4) {
+      if (first) TBK_STEP(true, false, 4); else TBK_STEP(false, false, 4);
     } else if (a.kst == 2) {
       if constexpr (CLS) return fail(TBK_ERR_UNSUPPORTED, "operator products in the class form");
       else { if (first) TBK_STEP(true, false, 2); else TBK_STEP(false, false, 2); }

@@ -336,7 +336,8 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     rec_bytes += 2 * vecb + ell_bytes(A, true);
     int g, t;
     TBK_TRY(step_config(A, Rc, prec, &g, &t, st));
-    return step_any(A, Rc, prec, x, y, nullptr, true, partd.as<double>(), g, t, st);
+    return step_any(A, Rc, prec, x, y, nullptr, true, partd.as<double>(), g, t, st, nullptr, 0, 0, true, nullptr,
+                    false);
   };
   auto round_to = [&](const void* src, float2* store, int32_t m) -> int {
     rec_bytes += vecb + stb;
@@ -382,7 +383,7 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
                            true, Aout));
         else
           TBK_TRY(step_any(Ht, Rc, prec, x, y, pv, m == 1, partd.as<double>(), grid, n_tiles, st,
-                           Aout ? nullptr : store, M, m, true));
+                           Aout ? nullptr : store, M, m, true, nullptr, false));
       }
       if (Aout && !fuse) TBK_TRY(apply_to_store(Aout, y, tmpA, store, m));
       else if (!Aout && m == 0) TBK_TRY(round_to(y, store, 0));

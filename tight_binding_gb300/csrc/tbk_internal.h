@@ -168,9 +168,10 @@ int step_config(tbk_sparse_s* A, int Rc, int prec, int* grid, int* n_tiles, cuda
 // block km of kM (store_y false: only there)
 // vop: with kstore, store vop x instead of the output; vop must share A's ELL
 // structure (same_ell_structure) and precision arrays
+// dots: form the moment partial sums (false: the step only feeds other work)
 int step_any(tbk_sparse_s* A, int Rc, int prec, const void* x, void* y, const void* pv, bool first, double* part,
              int grid, int n_tiles, cudaStream_t st, float2* kstore = nullptr, int32_t kM = 0, int32_t km = 0,
-             bool store_y = true, tbk_sparse_s* vop = nullptr);
+             bool store_y = true, tbk_sparse_s* vop = nullptr, bool dots = true);
 // ELL value / diagonal arrays of a precision (FP32, FP64 or double-float pairs)
 const void* ell_vals(const EllDev& E, int prec);
 const void* ell_diag(const EllDev& E, int prec);
