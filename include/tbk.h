@@ -368,9 +368,13 @@ enum {
                                        commutators do): same stored bits, one pass per
                                        block instead of two; opt-in: the wider step holds
                                        more registers and measured no faster            */
-  TBK_MU_BOTH_SIDES = 16            /* with TBK_MU_FUSED_OPS: run the left and right
+  TBK_MU_BOTH_SIDES = 16,           /* with TBK_MU_FUSED_OPS: run the left and right
                                        recursions as one of twice the width (same bits;
                                        opt-in, measured no faster)                      */
+  TBK_MU_FP64_BLOCKS = 32           /* the FP64 reference form: stored blocks kept in
+                                       complex128 and mu_nm formed by an FP64 CUDA-core
+                                       GEMM (twice the block memory, FP64-pipe bound);
+                                       ignores TBK_MU_TENSOR, FUSED_OPS, BOTH_SIDES     */
 };
 /* mu_mn = sum_{sites,r} conj(aL_m) aR_n with aL_m = g_m AL T_m(H~) BL |r>,
  * aR_n = g_n AR T_n(H~) BR |r> (NULL operator = identity), m, n < M: the stored

@@ -42,6 +42,7 @@ BUILD_BARE = 2
 MU_CUDA_CORE, MU_TENSOR, MU_MIXED_RECURSION, MU_DD_RECURSION = 0, 1, 2, 4
 MU_FUSED_OPS = 8
 MU_BOTH_SIDES = 16
+MU_FP64_BLOCKS = 32
 
 KERNEL_DIRICHLET, KERNEL_FEJER, KERNEL_LORENTZ, KERNEL_JACKSON, KERNEL_LANCZOS, KERNEL_WANG_ZUNGER = range(6)
 

@@ -101,6 +101,62 @@ __global__ void mu_split_reduce_kernel(const double2* __restrict__ part, int32_t
   acc[q].y += i;
 }
 
+// FP64 reference GEMM on complex128 K-tiled blocks: C[m][n] += sum_k
+// conj(L[m][k]) R[n][k] with every product and sum in FP64 (split-K partials,
+// reduced in a fixed order by mu_split_reduce_kernel).
+constexpr int kGK64 = 16;
+__global__ void __launch_bounds__(256) mu_gemm_f64_kernel(const double2* __restrict__ L,
+                                                          const double2* __restrict__ Rb, int32_t M, int64_t K,
+                                                          int64_t ksplit, double2* __restrict__ part) {
+  __shared__ double2 Ls[kGT][kGK64 + 1], Rs[kGT][kGK64 + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int32_t m0 = blockIdx.y * kGT, n0 = blockIdx.x * kGT;
+  const int64_t k0 = (int64_t)blockIdx.z * ksplit;
+  const int64_t k1 = min(K, k0 + ksplit);
+  double dr[2][2] = {{0, 0}, {0, 0}}, di[2][2] = {{0, 0}, {0, 0}};
+  for (int64_t kb = k0; kb < k1; kb += kGK64) {
+    for (int q = threadIdx.x; q < kGT * kGK64; q += 256) {
+      const int row = q / kGK64, kk = q % kGK64;
+      const int64_t k = kb + kk;
+      const double2 z = make_double2(0.0, 0.0);
+      Ls[row][kk] = (m0 + row < M && k < k1) ? L[((k >> 4) * M + (m0 + row)) * 16 + (k & 15)] : z;
+      Rs[row][kk] = (n0 + row < M && k < k1) ? Rb[((k >> 4) * M + (n0 + row)) * 16 + (k & 15)] : z;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < kGK64; ++kk) {
+      const double2 a[2] = {Ls[ty * 2][kk], Ls[ty * 2 + 1][kk]};
+      const double2 b[2] = {Rs[tx * 2][kk], Rs[tx * 2 + 1][kk]};
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          dr[i][j] = fma(a[i].x, b[j].x, fma(a[i].y, b[j].y, dr[i][j]));
+          di[i][j] = fma(a[i].x, b[j].y, fma(-a[i].y, b[j].x, di[i][j]));
+        }
+    }
+    __syncthreads();
+  }
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) {
+      const int32_t m = m0 + ty * 2 + i, n = n0 + tx * 2 + j;
+      if (m < M && n < M) part[((int64_t)blockIdx.z * M + m) * M + n] = make_double2(dr[i][j], di[i][j]);
+    }
+}
+
+// work block -> block m of a complex128 K-tiled store (the FP64 reference form)
+__device__ __forceinline__ double2 to_c128(double2 v) { return v; }
+__device__ __forceinline__ double2 to_c128(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ double2 to_c128(dd2 v) {
+  return make_double2((double)v.x.hi + (double)v.x.lo, (double)v.y.hi + (double)v.y.lo);
+}
+template <typename CT>
+__global__ void store_block64_kernel(const CT* __restrict__ src, double2* __restrict__ store, int32_t m, int32_t M,
+                                     int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    store[((q >> 4) * M + m) * 16 + (q & 15)] = to_c128(src[q]);
+}
+
 // work block -> block m of the complex64 K-tiled store (complex128 work blocks
 // are rounded once per element); 16 consecutive k form one contiguous 128-byte
 // row of the tile
@@ -266,9 +322,11 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     TBK_CUDA(cudaMemGetInfo(&fr, &tot));
     budget = 0.6 * (double)fr;
   }
-  while (Rc > 1 && 2.0 * M * n_pad * Rc * 8.0 > budget) Rc >>= 1;
-  if (2.0 * M * n_pad * Rc * 8.0 > budget)
-    return fail(TBK_ERR_BUDGET, "stored Chebyshev blocks need %.1f GB > budget %.1f GB", 2.0 * M * n_pad * 8.0 / 1e9,
+  const bool f64b = (flags & TBK_MU_FP64_BLOCKS) != 0;   // FP64 reference form: complex128 blocks, FP64 GEMM
+  const double sel = f64b ? 16.0 : 8.0;                   // bytes per stored element
+  while (Rc > 1 && 2.0 * M * n_pad * Rc * sel > budget) Rc >>= 1;
+  if (2.0 * M * n_pad * Rc * sel > budget)
+    return fail(TBK_ERR_BUDGET, "stored Chebyshev blocks need %.1f GB > budget %.1f GB", 2.0 * M * n_pad * sel / 1e9,
                 budget / 1e9);
   const int64_t blk = n_pad * Rc;                       // complex entries per block
   // stored blocks: complex64.  Recursion and operator applications: complex128
@@ -282,12 +340,12 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   const size_t csz = prec == TBK_PREC_MIXED ? sizeof(float2) : sizeof(double2);
   DevBuf Ls, Rs, work, partd, part, macc, gdev, kstage;
   const int64_t blk16 = (blk + 15) / 16 * 16;           // K padded to whole 16-element tiles (zeros)
-  TBK_TRY(Ls.alloc(sizeof(float2) * blk16 * M));
-  TBK_TRY(Rs.alloc(sizeof(float2) * blk16 * M));
+  TBK_TRY(Ls.alloc((size_t)sel * blk16 * M));
+  TBK_TRY(Rs.alloc((size_t)sel * blk16 * M));
   // both sides as one recursion of width 2 Rc (TBK_MU_BOTH_SIDES) when every
   // output operator can be fused into the step (the gathers move twice the
   // bytes per row; the stored values are the same bits)
-  bool both = (flags & TBK_MU_BOTH_SIDES) && (flags & TBK_MU_FUSED_OPS) &&
+  bool both = !f64b && (flags & TBK_MU_BOTH_SIDES) && (flags & TBK_MU_FUSED_OPS) &&
               2 * Rc <= (prec == TBK_PREC_MIXED ? 64 : 32) && (prec != TBK_PREC_MIXED || Rc >= 2);
   for (tbk_sparse_s* o : {AL, AR}) {
     if (!both || !o) continue;
@@ -348,6 +406,17 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     TBK_CHECK_LAUNCH();
     return TBK_OK;
   };
+  // FP64 reference form: block m of the complex128 store from a work block
+  auto store64 = [&](const void* src, void* store, int32_t m) -> int {
+    rec_bytes += vecb + 2 * stb;
+    const unsigned g = (unsigned)std::min<int64_t>((blk + 255) / 256, 65535);
+    double2* d = static_cast<double2*>(store);
+    if (prec == TBK_PREC_FP64) store_block64_kernel<double2><<<g, 256, 0, st>>>(static_cast<const double2*>(src), d, m, M, blk);
+    else if (prec == TBK_PREC_DD) store_block64_kernel<dd2><<<g, 256, 0, st>>>(static_cast<const dd2*>(src), d, m, M, blk);
+    else store_block64_kernel<float2><<<g, 256, 0, st>>>(static_cast<const float2*>(src), d, m, M, blk);
+    TBK_CHECK_LAUNCH();
+    return TBK_OK;
+  };
   // block m of `store` = A x, written by the product itself (no work block)
   auto apply_to_store = [&](tbk_sparse_s* A, const void* x, void* scratch, float2* store, int32_t m) -> int {
     rec_bytes += vecb + ell_bytes(A, true) + stb;
@@ -364,6 +433,25 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   auto side = [&](tbk_sparse_s* Aout, tbk_sparse_s* Bin, float2* store) -> int {
     void* r[3] = {wblk(0), wblk(1), wblk(2)};
     void* tmpA = wblk(3);
+    if (f64b) {                                           // recursion, operator, complex128 store
+      if (Bin) TBK_TRY(apply(Bin, v0, r[0]));
+      else TBK_CUDA(cudaMemcpyAsync(r[0], v0, csz * blk, cudaMemcpyDeviceToDevice, st));
+      for (int32_t m = 0; m < M; ++m) {
+        void* y = r[m % 3];
+        if (m >= 1) {
+          rec_bytes += (m >= 2 ? 3 : 2) * vecb + ell_bytes(Ht, true);
+          TBK_TRY(step_any(Ht, Rc, prec, r[(m - 1) % 3], y, m >= 2 ? r[(m - 2) % 3] : nullptr, m == 1,
+                           partd.as<double>(), grid, n_tiles, st, nullptr, 0, 0, true, nullptr, false));
+        }
+        if (Aout) {
+          TBK_TRY(apply(Aout, y, tmpA));
+          TBK_TRY(store64(tmpA, store, m));
+        } else {
+          TBK_TRY(store64(y, store, m));
+        }
+      }
+      return TBK_OK;
+    }
     bool fuse = false;
     if (Aout && (flags & TBK_MU_FUSED_OPS)) {
       TBK_TRY(same_ell_structure(Ht, Aout, &fuse, st));
@@ -453,8 +541,9 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     }
     return TBK_OK;
   };
-  const bool use_tc = (flags & TBK_MU_TENSOR) != 0;
-  const int64_t ksplit = 16384;
+  const bool use_tc = !f64b && (flags & TBK_MU_TENSOR) != 0;
+  // split-K: at least 16,384 K values per CTA, at most 64 partial M x M blocks
+  const int64_t ksplit = std::max<int64_t>(16384, (blk + 63) / 64);
   const int32_t nsplit = (int32_t)((blk + ksplit - 1) / ksplit);
   if (!use_tc) TBK_TRY(part.alloc(sizeof(double2) * (size_t)nsplit * M * M));
   cudaEvent_t ev[3];
@@ -471,7 +560,14 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
       TBK_TRY(side(AR, BR, Rs.as<float2>()));
     }
     TBK_CUDA(cudaEventRecord(ev[1], st));
-    if (use_tc) {
+    if (f64b) {
+      dim3 g((M + kGT - 1) / kGT, (M + kGT - 1) / kGT, nsplit);
+      mu_gemm_f64_kernel<<<g, 256, 0, st>>>(Ls.as<double2>(), Rs.as<double2>(), M, blk, ksplit, part.as<double2>());
+      TBK_CHECK_LAUNCH();
+      mu_split_reduce_kernel<<<(unsigned)(((int64_t)M * M + 255) / 256), 256, 0, st>>>(part.as<double2>(), M, nsplit,
+                                                                                       macc.as<double2>());
+      TBK_CHECK_LAUNCH();
+    } else if (use_tc) {
       TBK_TRY(mu_gemm_tc(Ls.as<float2>(), Rs.as<float2>(), M, blk, macc.as<double>(), st));
     } else {
       dim3 g((M + kGT - 1) / kGT, (M + kGT - 1) / kGT, nsplit);

@@ -28,14 +28,17 @@ _RECURSION = {"fp64": 0, "mixed": capi.MU_MIXED_RECURSION, "dd": capi.MU_DD_RECU
 
 def kubo_mu(Ht: SparseMatrix, AL=None, BL=None, AR=None, BR=None, M: int = 64, R: int = 4, seed: int = 0,
             kets=None, kernel: Kernel | None = None, tensor: bool = False, budget_gb: float = 0.0,
-            recursion: str = "dd", fuse_ops: bool = False, both_sides: bool = False) -> np.ndarray:
+            recursion: str = "dd", fuse_ops: bool = False, both_sides: bool = False,
+            fp64_blocks: bool = False) -> np.ndarray:
     """mu_mn = sum conj(g_m AL T_m BL r) (g_n AR T_n BR r); operators None = identity.
     recursion: "dd" (default; double-float work blocks: FP64-class accuracy on the
     FP32 pipe), "fp64" (complex128) or "mixed" (complex64, FP32 H~).  fuse_ops:
     form AL / AR products inside the recursion step when they share H~'s
     sparsity (same stored bits, one pass instead of two; opt-in, measured no
     faster); both_sides (with fuse_ops): run the two sides as one recursion of
-    twice the width (same bits)."""
+    twice the width (same bits).  fp64_blocks: the FP64 reference form —
+    complex128 stored blocks and an FP64 GEMM (tensor, fuse_ops and both_sides
+    are then ignored)."""
     kernel = kernel if kernel is not None else Dirichlet()
     mu = np.zeros((M, M), dtype=np.complex128)
     K = None
@@ -46,7 +49,8 @@ def kubo_mu(Ht: SparseMatrix, AL=None, BL=None, AR=None, BR=None, M: int = 64, R
                             None if K is None else capi.ptr(K), kernel.kind, kernel.p0, kernel.p1,
                             (capi.MU_TENSOR if tensor else capi.MU_CUDA_CORE) | _RECURSION[recursion]
                             | (capi.MU_FUSED_OPS if fuse_ops else 0)
-                            | (capi.MU_BOTH_SIDES if both_sides else 0),
+                            | (capi.MU_BOTH_SIDES if both_sides else 0)
+                            | (capi.MU_FP64_BLOCKS if fp64_blocks else 0),
                             float(budget_gb), capi.ptr(mu), None))
     return mu
 
@@ -105,7 +109,7 @@ def bastin_integrate(eps, zeta):
 def conductivity_Kubo_Bastin(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMatrix, N: int, E_min: float,
                              E_max: float, Volume: float = 1.0, R: int = 4, seed: int = 0, kernel: Kernel | None = None,
                              tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd", fuse_ops: bool = False,
-                             velocity=None):
+                             velocity=None, fp64_blocks: bool = False):
     """TB/snippets.h:306-456: G(N, H, E_min-1e-8, E_max+1e-8); v = X H~ - H~ X;
     aL = g T r, aR = g v_x T v_y r; zeta at the N Chebyshev nodes; cumulative
     integral from E = 0.  Returns dict with eps, zeta, E, sigma_re, sigma_im, mu.
@@ -120,7 +124,7 @@ def conductivity_Kubo_Bastin(H_og: SparseMatrix, op_x: SparseMatrix, op_y: Spars
         v_x = commutator(Ht, op_x)
         v_y = commutator(Ht, op_y)
     mu = kubo_mu(Ht, None, None, v_x, v_y, N, R, seed, kernel=kernel, tensor=tensor, budget_gb=budget_gb,
-                 recursion=recursion, fuse_ops=fuse_ops)
+                 recursion=recursion, fuse_ops=fuse_ops, fp64_blocks=fp64_blocks)
     eps = chebyshev_nodes(N)
     zeta = bastin_zeta(mu, eps, Volume)
     E, sr, si = bastin_integrate(eps, zeta)
@@ -129,7 +133,8 @@ def conductivity_Kubo_Bastin(H_og: SparseMatrix, op_x: SparseMatrix, op_y: Spars
 
 def conductivity_spectrum(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMatrix, N: int, R: int = 128,
                           seed: int = 0, kernel: Kernel | None = None, E_min: float = -4.0001, E_max: float = 4.0001,
-                          tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd", fuse_ops: bool = False):
+                          tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd", fuse_ops: bool = False,
+                          fp64_blocks: bool = False):
     """Kubo-Greenwood spectrum, TB/snippets.h:225-304: aR = g T r, aL = g v_x T v_x r,
     sigma(eps_k) = -<phi_L|phi_R> w(eps_k)^2 / R at the N Chebyshev nodes."""
     kernel = kernel if kernel is not None else Lorentz(6.0)
@@ -137,7 +142,7 @@ def conductivity_spectrum(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMa
     Ht = G.scaled_HE
     v_x = commutator(Ht, op_x)
     mu = kubo_mu(Ht, v_x, v_x, None, None, N, R, seed, kernel=kernel, tensor=tensor, budget_gb=budget_gb,
-                 recursion=recursion, fuse_ops=fuse_ops)
+                 recursion=recursion, fuse_ops=fuse_ops, fp64_blocks=fp64_blocks)
     eps = chebyshev_nodes(N)
     return eps, greenwood_sigma(mu, eps, R), mu
 
