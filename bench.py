@@ -152,6 +152,27 @@ def cpu_sample(cp, ri, v, n, steps, threads, R=R_VEC):
     return n * R * steps / dt, dt
 
 
+def reference_gpu_algorithm(N, cp, ri, v, kets_ptr, R, n_mom):
+    """The reference's own GPU algorithm (tight_binding/numerics_cuda.cu:190-255,
+    restated in baseline/cusparse_kpm.cu): per call the CSC and the split Re / Im
+    blocks are uploaded and the handles created; per moment two FP64 cuSPARSE
+    SpMMs and two blocking cublasDdot traces.  Host CSC and kets in, moments out."""
+    import ctypes as C
+
+    lib = C.CDLL(str(ROOT / "baseline" / "_build" / "libref_cusparse.so"))
+    fn = lib.ref_cusparse_braket_real
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                   C.c_int32, C.c_void_p, C.c_void_p]
+    mu = np.zeros(n_mom)
+    t = np.zeros(2)
+    rc = fn(N, len(ri), cp.ctypes.data, ri.ctypes.data, v.ctypes.data, n_mom, kets_ptr, kets_ptr, R, mu.ctypes.data,
+            t.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"reference cuSPARSE path failed at baseline/cusparse_kpm.cu:{rc}")
+    return mu, float(t[0]), float(t[1])
+
+
 def build_host_system():
     """The rescaled H~ of the workload as host CSC arrays (built on the device)."""
     import tight_binding_gb300 as tb
@@ -339,6 +360,18 @@ def run_gpu(args):
     ms64, nl64, b64 = fp.last_timing()
     del fp
 
+    # ---- the reference's GPU algorithm itself (cuSPARSE + cuBLAS per moment), same H~, kets and moments
+    ref_mu, ref_call_ms, ref_loop_ms = reference_gpu_algorithm(N, cp, ri, v, kets_p.data_ptr(), R_VEC, m64)
+    units64 = float(N) * m64 * R_VEC
+    reference_gpu = {
+        "algorithm": "tight_binding/numerics_cuda.cu:190-255 restated (baseline/cusparse_kpm.cu): per moment 2 FP64 "
+                     "cusparseSpMM (CSC, Re/Im blocks) + 2 blocking cublasDdot; CSC, blocks and handles per call",
+        "moments": m64, "call_ms": ref_call_ms, "loop_ms": ref_loop_ms,
+        "value_call": units64 / (ref_call_ms / 1e3), "value_loop": units64 / (ref_loop_ms / 1e3), "unit": UNIT,
+        "rel_err_vs_fp64_plain": float(np.max(np.abs(ref_mu - mu64)) / abs(mu64[0])),
+        "speedup_fp64_plain_over_it": ref_loop_ms / fp_ms,
+    }
+
     # ---- double-float plain path: the same algorithm with FP64-class accuracy on the FP32 pipe
     ddp = tb.KpmSolver(Ht, R_VEC, precision="dd", doubling=False, flags=capi.FLAG_DEVICE_PTRS)
     with torch.cuda.stream(stream):
@@ -397,6 +430,8 @@ def run_gpu(args):
         "fp64_plain": {"value": fp_value, "unit": UNIT, "moments": m64, "ms": fp_ms,
                        "kernel_ms": ms64, "launches": nl64, "bytes_per_launch": b64,
                        "speedup_mixed_over_fp64": value / fp_value},
+        "reference_gpu": dict(reference_gpu, speedup_mixed_over_it=value / reference_gpu["value_loop"],
+                              speedup_dd_plain_over_it=ref_loop_ms / dd_ms),
         "dd_plain": {"value": float(N) * m64 * R_VEC / (dd_ms / 1e3), "unit": UNIT, "moments": m64, "ms": dd_ms,
                      "kernel_GBps": bdd * nldd / (msdd / 1e3) / 1e9, "speedup_over_fp64_plain": fp_ms / dd_ms,
                      "rel_err_vs_fp64": float(np.max(np.abs(mudd - mu64)) / abs(mu64[0]))},

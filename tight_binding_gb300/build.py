@@ -99,8 +99,25 @@ def build_oracle() -> Path:
     return ROOT / "oracle" / "_build" / "libkpm_oracle.so"
 
 
+BASELINE_SRC = ROOT / "baseline" / "cusparse_kpm.cu"
+BASELINE_LIB = ROOT / "baseline" / "_build" / "libref_cusparse.so"
+
+
+def build_baseline() -> Path:
+    """The reference's cuSPARSE + cuBLAS moments algorithm restated as a timing
+    baseline (baseline/cusparse_kpm.cu); not linked into libtbk."""
+    if _stale(BASELINE_LIB, [BASELINE_SRC]):
+        BASELINE_LIB.parent.mkdir(parents=True, exist_ok=True)
+        _run([_nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", str(BASELINE_SRC),
+              "-o", str(BASELINE_LIB), "-lcusparse", "-lcublas", "-Xlinker", "-rpath=/usr/local/cuda/lib64"])
+    return BASELINE_LIB
+
+
 def build_all(verbose: bool = False) -> None:
-    build_library(verbose)
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        side = ex.submit(build_baseline)
+        build_library(verbose)
+        side.result()
     build_cpp_test()
     build_oracle()
 
