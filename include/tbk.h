@@ -303,6 +303,13 @@ int tbk_cheb_braket_complex(int32_t n_rows, int64_t nnz, const int32_t* col_ptr,
 /* Frees the matrix and plans cached by tbk_cheb_braket_* (no counterpart in
  * the reference, which keeps nothing between calls). */
 void tbk_cheb_braket_release(void);
+/* Polls a bounded device wait of the TMA-staged step kernel (TBK_FLAG_STAGED)
+ * makes before it gives up, records an error and lets the call return
+ * TBK_ERR_TIMEOUT; polls < 0 restores the default (2^24), 0 gives up at once.
+ * No counterpart in the reference (its kernels have no waits): it exists so a
+ * test can drive the failure path without hanging the GPU.  Copies already in
+ * flight are always waited for with the default limit. */
+int tbk_set_wait_limit(int64_t polls);
 
 /* Resident solver: H~ and the recursion state stay on the device between runs.
  * Replaces the per-call upload/alloc of TB/numerics_cuda.cu:199-222. */

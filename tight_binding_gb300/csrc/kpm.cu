@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cmath>
 #include <mutex>
@@ -132,6 +133,8 @@ __global__ void assemble_moments_kernel(const double* __restrict__ sums, int32_t
 
 
 constexpr int kTmaStages = 4;
+// polls of the staged kernel's ring waits before they give up (tbk_set_wait_limit)
+std::atomic<uint32_t> g_wait_limit{kWaitLimit};
 
 template <typename F, int R, bool CPLX_H, bool BRAKET>
 static int tma_kernel_setup(int smem, int* occ) {
@@ -152,14 +155,15 @@ static int launch_tma_r(const StepArgs& a, const TmaLayout& L, bool first, bool 
   auto b = static_cast<const CT*>(a.bras);
   auto ev = static_cast<const F*>(a.eval);
   auto dg = static_cast<const F*>(a.diag);
+  const uint32_t lim = g_wait_limit.load(std::memory_order_relaxed);
   if (braket)
     kpm_tma_step_kernel<F, R, CPLX_H, true, kTmaStages><<<grid, kTmaThreads, smem, st>>>(
         a.n, a.n_slices, a.n_tiles, L, a.soff, a.ecol, ev, dg, x, y, b, a.part, a.store, a.reverse, a.gather,
-        first ? 1 : 0, a.err);
+        first ? 1 : 0, a.err, lim);
   else
     kpm_tma_step_kernel<F, R, CPLX_H, false, kTmaStages><<<grid, kTmaThreads, smem, st>>>(
         a.n, a.n_slices, a.n_tiles, L, a.soff, a.ecol, ev, dg, x, y, b, a.part, a.store, a.reverse, a.gather,
-        first ? 1 : 0, a.err);
+        first ? 1 : 0, a.err, lim);
   TBK_CHECK_LAUNCH();
   return TBK_OK;
 }
@@ -1142,6 +1146,12 @@ static int cheb_braket_common(int32_t n_rows, int64_t nnz, const int32_t* cp, co
   tbk_kpm_destroy(P);
   tbk_sparse_destroy(H);
   return s;
+}
+
+int tbk_set_wait_limit(int64_t polls) {
+  if (polls > (int64_t)kWaitLimit) return fail(TBK_ERR_INVALID, "wait limit above %u polls", kWaitLimit);
+  g_wait_limit.store(polls < 0 ? kWaitLimit : (uint32_t)polls, std::memory_order_relaxed);
+  return TBK_OK;
 }
 
 void tbk_cheb_braket_release(void) {

@@ -11,9 +11,12 @@
 // hits), write v_{n+1} with coalesced 128-bit stores and fold the moment dot
 // products into the pass; then they arrive on the stage's "empty" mbarrier.
 //
-// Every wait is bounded: after kWaitLimit polls a wait records an error code in
-// a global flag and the CTA leaves; the producer first drains the copies it
-// still has in flight (again bounded), so no bulk copy outlives its CTA.
+// Every wait is bounded: after `wait_limit` polls (kWaitLimit unless the host
+// lowered it to exercise this path) a ring wait records an error code in a
+// global flag and the warp leaves its loop.  Before it leaves, the producer
+// always waits for the copies it still has in flight (bounded by kWaitLimit,
+// whatever wait_limit is: the copies are real reads that complete), so no bulk
+// copy outlives its CTA even when the consumers stopped early.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -49,9 +52,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait; returns false (and the caller records an error) on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < kWaitLimit; ++it)
+// Bounded wait; returns false (and the caller records an error) after `limit`
+// polls without completion (limit 0: no poll at all).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
+  for (uint32_t it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -118,7 +122,7 @@ __global__ void __launch_bounds__(kTmaThreads) kpm_tma_step_kernel(
     int32_t n, int32_t n_slices, int32_t n_tiles, TmaLayout L, const int32_t* __restrict__ soff, const int32_t* __restrict__ ecol,
     const F* __restrict__ eval, const F* __restrict__ diag, const typename C2<F>::T* __restrict__ x,
     typename C2<F>::T* y, const typename C2<F>::T* __restrict__ bras, double* __restrict__ part, int store,
-    int reverse, int gather, int first, int* __restrict__ err) {
+    int reverse, int gather, int first, int* __restrict__ err, uint32_t wait_limit) {
   using CT = typename C2<F>::T;
   constexpr int VPL = (R >= VecW<F>::max_vpl) ? VecW<F>::max_vpl : 1;
   constexpr int LPR = R / VPL;          // lanes per row
@@ -156,7 +160,7 @@ __global__ void __launch_bounds__(kTmaThreads) kpm_tma_step_kernel(
       for (int32_t k = 0; k < my_tiles; ++k) {
         const int st = k % STAGES;
         const uint32_t ph = (uint32_t)(k / STAGES) & 1u;
-        if (!mbar_wait_bounded(&empty_bar[st], ph ^ 1u)) { atomicOr(err, kErrEmptyWait); ok = false; break; }
+        if (!mbar_wait_bounded(&empty_bar[st], ph ^ 1u, wait_limit)) { atomicOr(err, kErrEmptyWait); ok = false; break; }
         const int32_t tile = tile_of(k);
         const int32_t r0 = tile * L.TR;
         const int32_t s0 = tile * slices_per_tile;
@@ -182,11 +186,12 @@ __global__ void __launch_bounds__(kTmaThreads) kpm_tma_step_kernel(
         bulk_g2s(sb + L.off_diag, diag + (size_t)r0 * HS, dbytes, &full_bar[st]);
         ++issued;
       }
-      if (!ok) {
-        // drain the copies still in flight before leaving (bounded)
-        for (int32_t k = issued - STAGES < 0 ? 0 : issued - STAGES; k < issued; ++k)
-          if (!mbar_wait_bounded(&full_bar[k % STAGES], (uint32_t)(k / STAGES) & 1u)) atomicOr(err, kErrDrain);
-      }
+      // wait for the copies still in flight before leaving (bounded): the
+      // consumers may have stopped early, and the CTA must not retire while a
+      // bulk copy still writes its shared memory
+      (void)ok;
+      for (int32_t k = issued - STAGES < 0 ? 0 : issued - STAGES; k < issued; ++k)
+        if (!mbar_wait_bounded(&full_bar[k % STAGES], (uint32_t)(k / STAGES) & 1u)) atomicOr(err, kErrDrain);
     }
     // producer warp contributes nothing to the moments
     return;
@@ -199,7 +204,7 @@ __global__ void __launch_bounds__(kTmaThreads) kpm_tma_step_kernel(
   for (int32_t k = 0; k < my_tiles; ++k) {
     const int st = k % STAGES;
     const uint32_t ph = (uint32_t)(k / STAGES) & 1u;
-    if (!mbar_wait_bounded(&full_bar[st], ph)) { atomicOr(err, kErrFullWait); break; }
+    if (!mbar_wait_bounded(&full_bar[st], ph, wait_limit)) { atomicOr(err, kErrFullWait); break; }
     const unsigned char* sb = smem + (size_t)st * L.stage_bytes;
     const CT* sx = reinterpret_cast<const CT*>(sb + L.off_x);
     const CT* sp = reinterpret_cast<const CT*>(sb + L.off_prev);
