@@ -23,3 +23,22 @@ def test_cpp_program(gpu):
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "ALL PASSED" in r.stdout, r.stdout
+
+
+def test_numerics_cuda_shim_compiles():
+    """include/tbk_numerics_cuda.hpp with the reference's declarations and the Eigen stand-in."""
+    from tight_binding_gb300 import build
+    r = subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-fsyntax-only", "-I", str(ROOT / "include"),
+                        "-I", str(ROOT / "tests" / "cpp" / "eigen_standin"), str(build.SHIM_TEST)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.gpu
+def test_numerics_cuda_shim_program(gpu):
+    """The shim's two overloads run the moments through libtbk (exact ring traces)."""
+    from tight_binding_gb300 import build
+    exe = build.build_shim_test()
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL PASSED" in r.stdout, r.stdout

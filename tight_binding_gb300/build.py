@@ -94,6 +94,21 @@ def build_cpp_test() -> Path:
     return CPP_TEST_BIN
 
 
+SHIM_TEST = ROOT / "tests" / "cpp" / "test_numerics_cuda_shim.cpp"
+SHIM_TEST_BIN = OUT / "test_numerics_cuda_shim"
+
+
+def build_shim_test() -> Path:
+    """The drop-in shim (include/tbk_numerics_cuda.hpp) compiled against the
+    Eigen stand-in, as the reference's numerics_cuda.cu would include it."""
+    deps = [SHIM_TEST, ROOT / "include" / "tbk_numerics_cuda.hpp", ROOT / "include" / "tbk.h", LIB]
+    if _stale(SHIM_TEST_BIN, deps):
+        _run([os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-Wall", "-I", str(ROOT / "include"),
+              "-I", str(ROOT / "tests" / "cpp" / "eigen_standin"), str(SHIM_TEST), "-L", str(OUT), "-ltbk",
+              "-Wl,-rpath,$ORIGIN", "-o", str(SHIM_TEST_BIN)])
+    return SHIM_TEST_BIN
+
+
 def build_oracle() -> Path:
     _run(["make", "-s", "-C", str(ROOT / "oracle")])
     return ROOT / "oracle" / "_build" / "libkpm_oracle.so"
@@ -119,6 +134,7 @@ def build_all(verbose: bool = False) -> None:
         build_library(verbose)
         side.result()
     build_cpp_test()
+    build_shim_test()
     build_oracle()
 
 
