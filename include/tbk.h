@@ -503,8 +503,9 @@ int tbk_request_footprint(const tbk_request* req, int64_t* build_peak_bytes,
  * bytes (max over builds of pool high-water minus reservation; <= 0 when
  * admission charged enough). */
 int tbk_server_stats(tbk_server server, double* out, int32_t n);
-/* Launch shape chosen per group, rows[5*i ..] = {precision, width, grid,
- * prefetch distance, ms per step}; returns the number of rows written. */
+/* Launch shape chosen per group, rows[6*i ..] = {precision, width, form (0:
+ * ELL, 1: row classes), grid, prefetch distance, ms per step}; returns the
+ * number of rows written. */
 int tbk_server_tuning(tbk_server server, int32_t max_rows, double* rows);
 
 /* =========================================================================

@@ -59,7 +59,9 @@ def test_requests_vs_oracle(gpu):
         st = srv.stats()
         assert st["done"] == len(CASES) and st["failed"] == 0
         assert st["reserved_bytes"] == 0
-        assert len(srv.tuning()) == 13
+        tun = srv.tuning()
+        assert len(tun) == 26                         # 13 (precision, width) groups, ELL and class form each
+        assert sum(t["form"] == "classes" for t in tun) == 13
 
 
 def _mix(tb, cells):

@@ -43,17 +43,21 @@ namespace {
 constexpr int kSrvThreads = 256;
 constexpr int kSrvWarps = kSrvThreads / 32;
 constexpr int kIterPerSlab = 8;        // warp iterations (512 B of v_s each) per slab
-constexpr int kGroups = 48;         // group code = (prec * 8 + log2(width)) * 2 + complex, prec < 3
+// group code = ((prec * 8 + log2(width)) * 2 + complex) * 2 + class form, prec < 3
+constexpr int kGroups = 96;
+using GroupMask = unsigned __int128;
+inline GroupMask group_bit(int code) { return (GroupMask)1 << code; }
 
 struct SLane {                      // up to 64 vectors of one request (device view)
-  const int32_t* soff;
-  const int32_t* ecol;
-  const void* eval;
+  const int32_t* soff;              // ELL slice offsets; class form: entry count per class
+  const int32_t* ecol;              // ELL columns; class form: column offsets per class
+  const void* eval;                 // ELL values; class form: values per class
   const void* diag;
+  const uint8_t* cls;               // class form: class of each row
   void* va;                         // v_s for even s
   void* vb;                         // v_s for odd s
   int32_t n, n_steps, s0, req;
-  int32_t slab_begin, n_slabs, slab_rows, pad;
+  int32_t slab_begin, n_slabs, slab_rows, cls_w;   // cls_w: class form, entries per class
 };
 struct SSlab {
   int32_t lane, row0;
@@ -88,7 +92,10 @@ inline int srv_slab_rows(int cs, int R, int64_t) { return srv_rows_per_warp(cs, 
 //   s == last:      no product, no store, partials <x|x>, <x|y_in>
 // which are the step sums of the doubling identities mu_2s = 2<v_s|v_s> - mu_0,
 // mu_2s-1 = 2<v_s|v_s-1> - mu_1.
-template <typename F, int R, bool CPLX_H>
+// CLS (a group of requests whose H~ has row classes): neighbours are row +
+// offset from the request's class table (read through L1), the row's class
+// byte is loaded one warp iteration ahead; no column index or value stream.
+template <typename F, int R, bool CPLX_H, bool CLS>
 __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_kernel(
     const SHdr* __restrict__ hdr, const SLane* __restrict__ lanes, const SSlab* __restrict__ slabs, int32_t g,
     int32_t j, int32_t reverse, int32_t pf_dist, double* __restrict__ part, int32_t slab_cap) {
@@ -103,7 +110,16 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
   const int sub = lane % LPR;
   const int32_t begin = hdr->grp_begin[g], cnt = hdr->grp_count[g];
   const int32_t nw = (int32_t)gridDim.x * kSrvWarps;
-  struct WP { const CT* x; CT* y; const int32_t* soff; const int32_t* ecol; const F* eval; const F* diag; };
+  struct WP {
+    const CT* x;
+    CT* y;
+    const int32_t* soff;
+    const int32_t* ecol;
+    const F* eval;
+    const F* diag;
+    const uint8_t* cls;
+    int32_t cw;
+  };
   __shared__ WP wp[kSrvWarps];
   volatile WP* my = wp + (threadIdx.x >> 5);
   for (int32_t t = (int32_t)blockIdx.x * kSrvWarps + (threadIdx.x >> 5); t < cnt; t += nw) {
@@ -138,15 +154,24 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
       my->ecol = L->ecol;
       my->eval = static_cast<const F*>(L->eval);
       my->diag = static_cast<const F*>(L->diag);
+      my->cls = L->cls;
+      my->cw = L->cls_w;
     }
     __syncwarp();
     const bool first = s == 0;
     const bool dot_only = s == ns - 1 && s > 0;
     const int32_t rend = min(sl.row0 + slab_rows, n);
     F m0 = 0, m1 = 0;
+    uint32_t c_next = 0;                       // class form: class of this lane's next row
+    if constexpr (CLS) {
+      const int32_t r0 = sl.row0 + lane / LPR;
+      if (r0 < rend) c_next = __ldg(my->cls + r0);
+    }
     for (int32_t rb = sl.row0; rb < rend; rb += RPW) {
       const int32_t r = rb + lane / LPR;
       if (r >= rend) break;
+      const uint32_t c_cur = c_next;
+      if constexpr (CLS) c_next = r + RPW < rend ? __ldg(my->cls + r + RPW) : 0u;
       const int64_t me = (int64_t)r * LPR + sub;
       const LaneV<F, VPL> xs = ld_ro<F, VPL>(my->x + me * VPL);
       LaneV<F, VPL> prev;
@@ -159,7 +184,30 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
       LaneV<F, VPL> acc;
 #pragma unroll
       for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
-      if (!dot_only) {
+      if (!dot_only && CLS) {
+        HVal<F, CPLX_H>::load(my->diag, r).template fma<VPL>(xs, acc);
+        const int32_t cw = my->cw;
+        const int32_t tb = (int32_t)c_cur * cw;
+        const int32_t cnt = __ldg(my->soff + c_cur);
+        const int32_t* co = my->ecol;
+        const F* cv = my->eval;
+        const CT* xp = my->x;
+        for (int k = 0; k < cnt; k += 4) {
+          HVal<F, CPLX_H> h[4];
+          LaneV<F, VPL> xv[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const bool v = k + u < cnt;
+            // rows are verified equal to their class: r + offset is the row's
+            // column; the clamp only keeps a bad table inside the block
+            const int32_t c = v ? min(max(r + __ldg(co + tb + k + u), 0), n - 1) : r;
+            h[u] = v ? HVal<F, CPLX_H>::load(cv, tb + k + u) : HVal<F, CPLX_H>::zero();
+            xv[u] = v ? ld_ro<F, VPL>(xp + ((int64_t)c * LPR + sub) * VPL) : xs;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
+        }
+      } else if (!dot_only) {
         HVal<F, CPLX_H>::load(my->diag, r).template fma<VPL>(xs, acc);
         const int32_t sidx = r >> 5, l = r & 31;
         const int32_t* so = my->soff;
@@ -296,17 +344,17 @@ struct LaunchArgs {
   double* part;
   int32_t code, j, reverse, pf, slab_cap, grid;
 };
-template <typename F, int R, bool C>
+template <typename F, int R, bool C, bool K>
 int srv_launch(const LaunchArgs& a, cudaStream_t st) {
-  srv_step_kernel<F, R, C><<<a.grid, kSrvThreads, 0, st>>>(a.hdr, a.lanes, a.slabs, a.code, a.j, a.reverse, a.pf,
-                                                          a.part, a.slab_cap);
+  srv_step_kernel<F, R, C, K><<<a.grid, kSrvThreads, 0, st>>>(a.hdr, a.lanes, a.slabs, a.code, a.j, a.reverse, a.pf,
+                                                             a.part, a.slab_cap);
   TBK_CHECK_LAUNCH();
   return TBK_OK;
 }
-template <typename F, int R, bool C>
+template <typename F, int R, bool C, bool K>
 int srv_occ() {
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, srv_step_kernel<F, R, C>, kSrvThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, srv_step_kernel<F, R, C, K>, kSrvThreads, 0);
   return nb > 0 ? nb : 1;
 }
 using LaunchFn = int (*)(const LaunchArgs&, cudaStream_t);
@@ -315,35 +363,41 @@ struct GroupFns {
   LaunchFn launch = nullptr;
   OccFn occ = nullptr;
 };
-template <typename F, bool C>
+template <typename F, bool C, bool K>
 GroupFns fns_for(int rc) {
   switch (rc) {
-    case 1: return {srv_launch<F, 1, C>, srv_occ<F, 1, C>};
-    case 2: return {srv_launch<F, 2, C>, srv_occ<F, 2, C>};
-    case 4: return {srv_launch<F, 4, C>, srv_occ<F, 4, C>};
-    case 8: return {srv_launch<F, 8, C>, srv_occ<F, 8, C>};
-    case 16: return {srv_launch<F, 16, C>, srv_occ<F, 16, C>};
-    case 32: return {srv_launch<F, 32, C>, srv_occ<F, 32, C>};
+    case 1: return {srv_launch<F, 1, C, K>, srv_occ<F, 1, C, K>};
+    case 2: return {srv_launch<F, 2, C, K>, srv_occ<F, 2, C, K>};
+    case 4: return {srv_launch<F, 4, C, K>, srv_occ<F, 4, C, K>};
+    case 8: return {srv_launch<F, 8, C, K>, srv_occ<F, 8, C, K>};
+    case 16: return {srv_launch<F, 16, C, K>, srv_occ<F, 16, C, K>};
+    case 32: return {srv_launch<F, 32, C, K>, srv_occ<F, 32, C, K>};
     case 64:
-      if constexpr (sizeof(F) == 4) return {srv_launch<F, 64, C>, srv_occ<F, 64, C>};
+      if constexpr (sizeof(F) == 4) return {srv_launch<F, 64, C, K>, srv_occ<F, 64, C, K>};
       break;
   }
   return {};
 }
-int code_prec(int code) { return code >> 4; }
-int code_width(int code) { return 1 << ((code >> 1) & 7); }
-bool code_cplx(int code) { return (code & 1) != 0; }
-int group_code(int prec, int rc, bool cplx) {
+int code_prec(int code) { return code >> 5; }
+int code_width(int code) { return 1 << ((code >> 2) & 7); }
+bool code_cplx(int code) { return (code & 2) != 0; }
+bool code_cls(int code) { return (code & 1) != 0; }
+int group_code(int prec, int rc, bool cplx, bool cls) {
   int lg = 0;
   while ((1 << lg) < rc) ++lg;
-  return ((prec * 8) + lg) * 2 + (cplx ? 1 : 0);
+  return (((prec * 8) + lg) * 2 + (cplx ? 1 : 0)) * 2 + (cls ? 1 : 0);
+}
+template <typename F>
+GroupFns fns_prec(int rc, bool c, bool k) {
+  if (k) return c ? fns_for<F, true, true>(rc) : fns_for<F, false, true>(rc);
+  return c ? fns_for<F, true, false>(rc) : fns_for<F, false, false>(rc);
 }
 GroupFns group_fns(int code) {
   const int rc = code_width(code);
-  const bool c = code_cplx(code);
-  if (code_prec(code) == TBK_PREC_MIXED) return c ? fns_for<float, true>(rc) : fns_for<float, false>(rc);
-  if (code_prec(code) == TBK_PREC_DD) return c ? fns_for<dd, true>(rc) : fns_for<dd, false>(rc);
-  return c ? fns_for<double, true>(rc) : fns_for<double, false>(rc);
+  const bool c = code_cplx(code), k = code_cls(code);
+  if (code_prec(code) == TBK_PREC_MIXED) return fns_prec<float>(rc, c, k);
+  if (code_prec(code) == TBK_PREC_DD) return fns_prec<dd>(rc, c, k);
+  return fns_prec<double>(rc, c, k);
 }
 int width_for(int prec, int R) {
   const int rmax = prec == TBK_PREC_MIXED ? 64 : 32;
@@ -550,7 +604,7 @@ struct tbk_server_s {
   char* stage[2] = {nullptr, nullptr};
   cudaEvent_t copy_ev[2] = {nullptr, nullptr};
   bool copy_pending[2] = {false, false};
-  std::map<std::pair<uint64_t, int>, cudaGraphExec_t> graphs;   // key: (group mask, round length)
+  std::map<std::pair<GroupMask, int>, cudaGraphExec_t> graphs;   // key: (group mask, round length)
   // launch shapes per group code
   int grid[kGroups] = {};
   int pf[kGroups] = {};
@@ -619,20 +673,29 @@ int build_request(tbk_server_s* S, SrvRequest* r) {
   if (s != TBK_OK) return s;
   r->Ht = Ht;
   TBK_TRY(ensure_ell(Ht, st));
-  // keep what the recursion reads: the ELL in the request's precision
+  // keep what the recursion reads: the ELL (or the row classes) in the request's precision
   Ht->col_ptr.release();
   Ht->row_idx.release();
   Ht->values.release();
+  TBK_TRY(ensure_classes(Ht, st));
   const bool mixed = q.precision == TBK_PREC_MIXED;
+  const bool cls = Ht->ell.cls_state == 1;
   if (q.precision == TBK_PREC_DD) TBK_TRY(ensure_ell_dd(Ht, st));
-  if (q.precision != TBK_PREC_FP64) { Ht->ell.val64.release(); Ht->ell.diag64.release(); }
-  if (!mixed) { Ht->ell.val32.release(); Ht->ell.diag32.release(); }
+  if (q.precision != TBK_PREC_FP64) { Ht->ell.val64.release(); Ht->ell.diag64.release(); Ht->ell.cls_v64.release(); }
+  if (!mixed) { Ht->ell.val32.release(); Ht->ell.diag32.release(); Ht->ell.cls_v32.release(); }
+  if (q.precision != TBK_PREC_DD) Ht->ell.cls_vdd.release();
+  if (cls) {                                  // the class form reads no ELL columns or values
+    Ht->ell.col.release();
+    Ht->ell.val64.release();
+    Ht->ell.val32.release();
+    Ht->ell.valdd.release();
+  }
   r->n = Ht->rows;
   r->rc = width_for(q.precision, q.R);
   r->cs = mixed ? 8 : 16;
   r->n_lanes = (q.R + r->rc - 1) / r->rc;
   r->n_steps = steps_for(q.n_mom);
-  r->code = group_code(q.precision, r->rc, Ht->ell.cplx != 0);
+  r->code = group_code(q.precision, r->rc, Ht->ell.cplx != 0, cls);
   r->slab_rows = srv_slab_rows(r->cs, r->rc, r->n);
   const int64_t Np = (int64_t)Ht->ell.n_slices * 32;
   const size_t blk = (size_t)Np * r->rc * r->cs;
@@ -650,11 +713,15 @@ int build_request(tbk_server_s* S, SrvRequest* r) {
   cudaMemPoolGetAttribute(S->pool, cudaMemPoolAttrUsedMemHigh, &high);
   const int64_t over = (int64_t)high - (int64_t)used0 - r->fp.peak;
   const EllDev& E = Ht->ell;
-  int64_t held = (int64_t)(E.slice_off.bytes + E.col.bytes + E.val32.bytes + E.val64.bytes + E.diag32.bytes +
-                           E.diag64.bytes + r->sums.bytes);
+  int64_t held = (int64_t)(E.slice_off.bytes + E.col.bytes + E.val32.bytes + E.val64.bytes + E.valdd.bytes +
+                           E.diag32.bytes + E.diag64.bytes + E.diagdd.bytes + E.cls.bytes + E.cls_cnt.bytes +
+                           E.cls_off.bytes + E.cls_v32.bytes + E.cls_v64.bytes + E.cls_vdd.bytes + r->sums.bytes);
   for (auto& v : r->vec) held += (int64_t)v.bytes;
   const double hv = (mixed ? 4.0 : 8.0) * (E.cplx ? 2.0 : 1.0);
-  r->mat_bytes = (double)E.n_entries * (4.0 + hv) + (double)E.n_rows * hv + 4.0 * (E.n_slices + 1);
+  // algorithmic matrix bytes of a step: the class byte and diagonal of each
+  // row (class form) or the ELL columns, values and diagonal
+  r->mat_bytes = cls ? (double)E.n_rows * (1.0 + hv)
+                     : (double)E.n_entries * (4.0 + hv) + (double)E.n_rows * hv + 4.0 * (E.n_slices + 1);
   r->vec_bytes = (double)r->n * r->rc * r->cs;
   r->step_bytes = r->n_lanes * (3.0 * r->vec_bytes + r->mat_bytes);
   std::lock_guard<std::mutex> lk(S->mu);
@@ -794,8 +861,8 @@ int ensure_tables(tbk_server_s* S, int32_t lanes, int32_t slabs, int32_t reqs) {
   return TBK_OK;
 }
 
-int capture_graph(tbk_server_s* S, uint64_t mask, int steps, cudaGraphExec_t* out) {
-  const std::pair<uint64_t, int> key(mask, steps);
+int capture_graph(tbk_server_s* S, GroupMask mask, int steps, cudaGraphExec_t* out) {
+  const std::pair<GroupMask, int> key(mask, steps);
   auto it = S->graphs.find(key);
   if (it != S->graphs.end()) { *out = it->second; return TBK_OK; }
   std::lock_guard<std::mutex> cap(S->capture_mu);
@@ -811,7 +878,7 @@ int capture_graph(tbk_server_s* S, uint64_t mask, int steps, cudaGraphExec_t* ou
   int rc = TBK_OK;
   cudaError_t e = cudaEventRecord(S->ev_fork, st);
   for (int code = 0; code < kGroups && e == cudaSuccess && rc == TBK_OK; ++code) {
-    if (!(mask & (1ull << code))) continue;
+    if (!(mask & group_bit(code))) continue;
     const GroupFns fn = group_fns(code);
     if (!fn.launch) { rc = fail(TBK_ERR_UNSUPPORTED, "group %d not instantiated", code); break; }
     cudaStream_t sd = S->side[code];
@@ -907,12 +974,12 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
   SReq* reqs = reinterpret_cast<SReq*>(hb + S->off_reqs);
   memset(hdr, 0, sizeof(SHdr));
   Round rd;
-  uint64_t mask = 0;
+  GroupMask mask = 0;
   int32_t li = 0, si = 0;
   for (int32_t qi = 0; qi < n_reqs; ++qi) {
     SrvRequest* r = order[qi];
     const int code = r->code;
-    if (!(mask & (1ull << code))) { mask |= 1ull << code; hdr->grp_begin[code] = si; }
+    if (!(mask & group_bit(code))) { mask |= group_bit(code); hdr->grp_begin[code] = si; }
     const int32_t sr = r->slab_rows;
     const int32_t steps = std::min(RS, r->n_steps - r->s0);
     SReq& q = reqs[qi];
@@ -927,10 +994,20 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
     const EllDev& E = r->Ht->ell;
     for (int32_t c = 0; c < r->n_lanes; ++c) {
       SLane& L = lanes[li];
-      L.soff = E.slice_off.as<int32_t>();
-      L.ecol = E.col.as<int32_t>();
       const int pq = r->q.precision;
-      L.eval = pq == TBK_PREC_MIXED ? E.val32.p : pq == TBK_PREC_DD ? E.valdd.p : E.val64.p;
+      if (E.cls_state == 1) {
+        L.soff = E.cls_cnt.as<int32_t>();
+        L.ecol = E.cls_off.as<int32_t>();
+        L.eval = pq == TBK_PREC_MIXED ? E.cls_v32.p : pq == TBK_PREC_DD ? E.cls_vdd.p : E.cls_v64.p;
+        L.cls = E.cls.as<uint8_t>();
+        L.cls_w = E.cls_w;
+      } else {
+        L.soff = E.slice_off.as<int32_t>();
+        L.ecol = E.col.as<int32_t>();
+        L.eval = pq == TBK_PREC_MIXED ? E.val32.p : pq == TBK_PREC_DD ? E.valdd.p : E.val64.p;
+        L.cls = nullptr;
+        L.cls_w = 0;
+      }
       L.diag = pq == TBK_PREC_MIXED ? E.diag32.p : pq == TBK_PREC_DD ? E.diagdd.p : E.diag64.p;
       L.va = r->vec[2 * c].p;
       L.vb = r->vec[2 * c + 1].p;
@@ -941,7 +1018,6 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
       L.slab_begin = si;
       L.n_slabs = (r->n + sr - 1) / sr;
       L.slab_rows = sr;
-      L.pad = 0;
       for (int32_t k = 0; k < L.n_slabs; ++k) slabs[si + k] = SSlab{li, k * sr};
       si += L.n_slabs;
       ++li;
@@ -975,7 +1051,7 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
   TBK_CUDA(cudaGraphLaunch(gx, st));
   TBK_CUDA(cudaEventRecord(rd.ev1, st));
   int groups = 0;
-  for (int c = 0; c < kGroups; ++c) groups += (int)((mask >> c) & 1);
+  for (int c = 0; c < kGroups; ++c) groups += (int)((mask >> c) & 1u);
   rd.launches = (int64_t)groups * RS + 2;
   // advance: who is left for the next round
   std::vector<SrvRequest*> next;
@@ -1050,7 +1126,10 @@ void loop_main(tbk_server_s* S) {
 
 // Times each candidate launch shape of every real group on a synthetic width-4
 // operator of ~64 MB per vector block (TBK_SERVE_TUNE_MB overrides) and keeps
-// the fastest (grid, prefetch distance).
+// the fastest (grid, prefetch distance).  Each width is tuned twice: through
+// the synthetic ELL, and in the class form with the same couplings as one
+// class (offsets +-1, +-257, clamped at the ends of the block); the complex-H
+// group of the same width and form takes the same shape.
 int autotune(tbk_server_s* S) {
   cudaStream_t st = S->st_loop;
   cudaEvent_t e0, e1;
@@ -1058,9 +1137,7 @@ int autotune(tbk_server_s* S) {
   TBK_CUDA(cudaEventCreate(&e1));
   int rc_all = TBK_OK;
   for (int prec = 0; prec < 3 && rc_all == TBK_OK; ++prec) {
-    for (int rc = 4; rc <= (prec == TBK_PREC_MIXED ? 64 : 32); rc <<= 1) {
-      const int code = group_code(prec, rc, false);
-      const GroupFns fn = group_fns(code);
+    for (int rc = 4; rc <= (prec == TBK_PREC_MIXED ? 64 : 32) && rc_all == TBK_OK; rc <<= 1) {
       const int cs = prec == TBK_PREC_MIXED ? 8 : 16;
       int64_t tune_mb = 64;
       if (const char* ev = getenv("TBK_SERVE_TUNE_MB")) tune_mb = std::max(1, atoi(ev));   // tuning override
@@ -1068,89 +1145,108 @@ int autotune(tbk_server_s* S) {
       const int sr = srv_slab_rows(cs, rc, n);
       n = std::max(sr, n / sr * sr);
       const int32_t ns = n / 32, n_slab = n / sr;
-      DevBuf soff, ecol, eval, diag, va, vb, tab, prt;
+      DevBuf soff, ecol, eval, diag, va, vb, tab, prt, ccnt, coff, cval, cls;
       const size_t fs = prec == TBK_PREC_MIXED ? 4 : 8;
       if ((rc_all = soff.alloc(4 * (size_t)(ns + 1))) || (rc_all = ecol.alloc(4 * 128 * (size_t)ns)) ||
           (rc_all = eval.alloc(fs * 128 * (size_t)ns)) || (rc_all = diag.alloc(fs * 32 * (size_t)ns)) ||
           (rc_all = va.alloc((size_t)n * rc * cs)) || (rc_all = vb.alloc((size_t)n * rc * cs)) ||
-          (rc_all = prt.alloc(sizeof(double) * 2 * (size_t)n_slab)))
+          (rc_all = prt.alloc(sizeof(double) * 2 * (size_t)n_slab)) || (rc_all = ccnt.alloc(sizeof(int32_t))) ||
+          (rc_all = coff.alloc(4 * sizeof(int32_t))) || (rc_all = cval.alloc(4 * fs)) ||
+          (rc_all = cls.alloc((size_t)n)))
         break;
       const int T = 256;
       if (prec == TBK_PREC_MIXED)
         srv_synth_ell_kernel<float><<<(ns * 32 + T) / T, T, 0, st>>>(n, ns, soff.as<int32_t>(), ecol.as<int32_t>(),
                                                                     eval.as<float>(), diag.as<float>());
+      else if (prec == TBK_PREC_DD)
+        srv_synth_ell_kernel<dd><<<(ns * 32 + T) / T, T, 0, st>>>(n, ns, soff.as<int32_t>(), ecol.as<int32_t>(),
+                                                                 eval.as<dd>(), diag.as<dd>());
       else
-        if (prec == TBK_PREC_DD)
-          srv_synth_ell_kernel<dd><<<(ns * 32 + T) / T, T, 0, st>>>(n, ns, soff.as<int32_t>(), ecol.as<int32_t>(),
-                                                                   eval.as<dd>(), diag.as<dd>());
-        else
         srv_synth_ell_kernel<double><<<(ns * 32 + T) / T, T, 0, st>>>(n, ns, soff.as<int32_t>(), ecol.as<int32_t>(),
                                                                      eval.as<double>(), diag.as<double>());
       TBK_CUDA(cudaGetLastError());
+      {
+        const int32_t hc = 4, ho[4] = {1, -1, 257, -257};
+        const float v32[4] = {0.25f, 0.25f, 0.25f, 0.25f};
+        const double v64[4] = {0.25, 0.25, 0.25, 0.25};
+        const float vdd[8] = {0.25f, 0.f, 0.25f, 0.f, 0.25f, 0.f, 0.25f, 0.f};   // (hi, lo) pairs
+        const void* hv = prec == TBK_PREC_MIXED ? (const void*)v32 : prec == TBK_PREC_DD ? (const void*)vdd
+                                                                                        : (const void*)v64;
+        TBK_CUDA(cudaMemcpyAsync(ccnt.p, &hc, sizeof(hc), cudaMemcpyHostToDevice, st));
+        TBK_CUDA(cudaMemcpyAsync(coff.p, ho, sizeof(ho), cudaMemcpyHostToDevice, st));
+        TBK_CUDA(cudaMemcpyAsync(cval.p, hv, 4 * fs, cudaMemcpyHostToDevice, st));
+        TBK_CUDA(cudaMemsetAsync(cls.p, 0, cls.bytes, st));
+      }
       TBK_CUDA(cudaMemsetAsync(vb.p, 0, vb.bytes, st));
       TBK_TRY(random_block_any(prec, n, rc, 0, rc, 7, va.p, st));
-      // table: one lane at step 1 of a long recursion, all its slabs in group `code`
       const size_t off_l = (sizeof(SHdr) + 255) & ~(size_t)255, off_s = off_l + ((sizeof(SLane) + 255) & ~(size_t)255);
-      std::vector<char> h(off_s + sizeof(SSlab) * (size_t)n_slab, 0);
-      SHdr* hd = reinterpret_cast<SHdr*>(h.data());
-      hd->grp_begin[code] = 0;
-      hd->grp_count[code] = n_slab;
-      hd->n_lanes = 1;
-      hd->n_slabs = n_slab;
-      SLane* L = reinterpret_cast<SLane*>(h.data() + off_l);
-      L->soff = soff.as<int32_t>();
-      L->ecol = ecol.as<int32_t>();
-      L->eval = eval.p;
-      L->diag = diag.p;
-      L->va = va.p;
-      L->vb = vb.p;
-      L->n = n;
-      L->n_steps = 1 << 30;
-      L->s0 = 1;
-      L->slab_begin = 0;
-      L->n_slabs = n_slab;
-      L->slab_rows = sr;
-      SSlab* sl = reinterpret_cast<SSlab*>(h.data() + off_s);
-      for (int32_t k = 0; k < n_slab; ++k) sl[k] = SSlab{0, k * sr};
-      TBK_TRY(tab.alloc(h.size()));
-      TBK_CUDA(cudaMemcpyAsync(tab.p, h.data(), h.size(), cudaMemcpyHostToDevice, st));
-      TBK_CUDA(cudaStreamSynchronize(st));
-      LaunchArgs a;
-      a.hdr = tab.as<SHdr>();
-      a.lanes = reinterpret_cast<const SLane*>(tab.as<char>() + off_l);
-      a.slabs = reinterpret_cast<const SSlab*>(tab.as<char>() + off_s);
-      a.part = prt.as<double>();
-      a.slab_cap = n_slab;
-      a.code = code;
-      a.j = 0;
-      const int occ = fn.occ();
-      const int grids[4] = {S->sms, 2 * S->sms, 4 * S->sms, occ * S->sms};
-      double best = 1e30;
-      for (int gi = 0; gi < 4; ++gi) {
-        if (grids[gi] > occ * S->sms) continue;
-        for (int pf = 0; pf <= 2; ++pf) {
-          a.grid = grids[gi];
-          a.pf = pf;
-          for (int w = 0; w < 2; ++w) { a.reverse = w & 1; TBK_TRY(fn.launch(a, st)); }
-          TBK_CUDA(cudaEventRecord(e0, st));
-          for (int w = 0; w < 6; ++w) { a.reverse = w & 1; TBK_TRY(fn.launch(a, st)); }
-          TBK_CUDA(cudaEventRecord(e1, st));
-          TBK_CUDA(cudaEventSynchronize(e1));
-          float ms = 0.f;
-          cudaEventElapsedTime(&ms, e0, e1);
-          if (ms / 6.0 < best) {
-            best = ms / 6.0;
-            S->grid[code] = a.grid;
-            S->pf[code] = pf;
+      TBK_TRY(tab.alloc(off_s + sizeof(SSlab) * (size_t)n_slab));
+      for (int form = 0; form < 2; ++form) {
+        const bool cf = form == 1;
+        const int code = group_code(prec, rc, false, cf);
+        const GroupFns fn = group_fns(code);
+        // table: one lane at step 1 of a long recursion, all its slabs in group `code`
+        std::vector<char> h(off_s + sizeof(SSlab) * (size_t)n_slab, 0);
+        SHdr* hd = reinterpret_cast<SHdr*>(h.data());
+        hd->grp_begin[code] = 0;
+        hd->grp_count[code] = n_slab;
+        hd->n_lanes = 1;
+        hd->n_slabs = n_slab;
+        SLane* L = reinterpret_cast<SLane*>(h.data() + off_l);
+        L->soff = cf ? ccnt.as<int32_t>() : soff.as<int32_t>();
+        L->ecol = cf ? coff.as<int32_t>() : ecol.as<int32_t>();
+        L->eval = cf ? cval.p : eval.p;
+        L->cls = cf ? cls.as<uint8_t>() : nullptr;
+        L->cls_w = cf ? 4 : 0;
+        L->diag = diag.p;
+        L->va = va.p;
+        L->vb = vb.p;
+        L->n = n;
+        L->n_steps = 1 << 30;
+        L->s0 = 1;
+        L->slab_begin = 0;
+        L->n_slabs = n_slab;
+        L->slab_rows = sr;
+        SSlab* sl = reinterpret_cast<SSlab*>(h.data() + off_s);
+        for (int32_t k = 0; k < n_slab; ++k) sl[k] = SSlab{0, k * sr};
+        TBK_CUDA(cudaMemcpyAsync(tab.p, h.data(), h.size(), cudaMemcpyHostToDevice, st));
+        TBK_CUDA(cudaStreamSynchronize(st));
+        LaunchArgs a;
+        a.hdr = tab.as<SHdr>();
+        a.lanes = reinterpret_cast<const SLane*>(tab.as<char>() + off_l);
+        a.slabs = reinterpret_cast<const SSlab*>(tab.as<char>() + off_s);
+        a.part = prt.as<double>();
+        a.slab_cap = n_slab;
+        a.code = code;
+        a.j = 0;
+        const int occ = fn.occ();
+        const int grids[4] = {S->sms, 2 * S->sms, 4 * S->sms, occ * S->sms};
+        double best = 1e30;
+        for (int gi = 0; gi < 4; ++gi) {
+          if (grids[gi] > occ * S->sms) continue;
+          for (int pf = 0; pf <= 2; ++pf) {
+            a.grid = grids[gi];
+            a.pf = pf;
+            for (int w = 0; w < 2; ++w) { a.reverse = w & 1; TBK_TRY(fn.launch(a, st)); }
+            TBK_CUDA(cudaEventRecord(e0, st));
+            for (int w = 0; w < 6; ++w) { a.reverse = w & 1; TBK_TRY(fn.launch(a, st)); }
+            TBK_CUDA(cudaEventRecord(e1, st));
+            TBK_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms / 6.0 < best) {
+              best = ms / 6.0;
+              S->grid[code] = a.grid;
+              S->pf[code] = pf;
+            }
           }
         }
+        S->tune_ms[code] = best;
+        S->tuned[code] = true;
+        const int cc = group_code(prec, rc, true, cf);
+        S->grid[cc] = S->grid[code];
+        S->pf[cc] = S->pf[code];
       }
-      S->tune_ms[code] = best;
-      S->tuned[code] = true;
-      // the complex-H group of the same width takes the same shape
-      const int cc = group_code(prec, rc, true);
-      S->grid[cc] = S->grid[code];
-      S->pf[cc] = S->pf[code];
       TBK_CUDA(cudaStreamSynchronize(st));
     }
   }
@@ -1369,12 +1465,13 @@ int tbk_server_tuning(tbk_server S, int32_t max_rows, double* rows) {
   int k = 0;
   for (int code = 0; code < kGroups && k < max_rows; ++code) {
     if (!S->tuned[code]) continue;
-    double* r = rows + 5 * k;
+    double* r = rows + 6 * k;
     r[0] = code_prec(code);
     r[1] = code_width(code);
-    r[2] = S->grid[code];
-    r[3] = S->pf[code];
-    r[4] = S->tune_ms[code];
+    r[2] = code_cls(code) ? 1 : 0;
+    r[3] = S->grid[code];
+    r[4] = S->pf[code];
+    r[5] = S->tune_ms[code];
     ++k;
   }
   return k;

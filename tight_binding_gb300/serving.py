@@ -168,11 +168,12 @@ class DosServer:
         return dict(zip(STATS_KEYS, v.tolist()))
 
     def tuning(self) -> list[dict]:
-        rows = np.zeros((64, 5), dtype=np.float64)
-        k = lib().tbk_server_tuning(self._h, 64, capi.ptr(rows))
+        rows = np.zeros((128, 6), dtype=np.float64)
+        k = lib().tbk_server_tuning(self._h, 128, capi.ptr(rows))
         names = {capi.PREC_MIXED: "mixed", capi.PREC_FP64: "fp64", capi.PREC_DD: "dd"}
-        return [dict(precision=names.get(int(r[0]), str(int(r[0]))), width=int(r[1]), grid=int(r[2]),
-                     prefetch=int(r[3]), ms_per_step=float(r[4])) for r in rows[:max(k, 0)]]
+        return [dict(precision=names.get(int(r[0]), str(int(r[0]))), width=int(r[1]),
+                     form="classes" if int(r[2]) else "ell", grid=int(r[3]), prefetch=int(r[4]),
+                     ms_per_step=float(r[5])) for r in rows[:max(k, 0)]]
 
     def close(self) -> None:
         h = getattr(self, "_h", None)
