@@ -96,7 +96,7 @@ inline int srv_slab_rows(int cs, int R, int64_t) { return srv_rows_per_warp(cs, 
 // offset from the request's class table (read through L1), the row's class
 // byte is loaded one warp iteration ahead; no column index or value stream.
 template <typename F, int R, bool CPLX_H, bool CLS>
-__global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_kernel(
+__global__ void __launch_bounds__(kSrvThreads, (sizeof(F) == 4 && !CLS) ? 5 : 4) srv_step_kernel(
     const SHdr* __restrict__ hdr, const SLane* __restrict__ lanes, const SSlab* __restrict__ slabs, int32_t g,
     int32_t j, int32_t reverse, int32_t pf_dist, double* __restrict__ part, int32_t slab_cap) {
   using CT = typename C2<F>::T;
