@@ -491,7 +491,7 @@ def peaks_tensor():
     return 1900.0 / 2.0, "half of fallback bf16"
 
 
-def run_kubo(config: int, tensor: bool = True, recursion: str = "dd", fuse_ops: bool = False, moments: int = 0,
+def run_kubo(config: int, tensor: bool = True, recursion: str = "mixed", fuse_ops: bool = False, moments: int = 0,
              budget_gb: float = 0.0, parity: bool = False):
     """Kubo legs: config 3 (Bastin sigma_xy, square 256^2 open-x / periodic-y, Landau
     flux 1/64, M = 512, R = 16, seed 2) or config 5 (Greenwood sigma_xx, FCC 128^3
@@ -889,8 +889,8 @@ def main():
     ap.add_argument("--kubo", type=int, default=0, choices=[0, 3, 5],
                     help="run only the Kubo leg of config 3 (sigma_xy) or 5 (sigma_xx)")
     ap.add_argument("--cuda-core-mu", action="store_true", help="Kubo leg with the CUDA-core mu GEMM")
-    ap.add_argument("--kubo-recursion", default="dd", choices=["fp64", "mixed", "dd"],
-                    help="stored-block recursion: double-float (default), complex128 or complex64")
+    ap.add_argument("--kubo-recursion", default="mixed", choices=["fp64", "mixed", "dd"],
+                    help="stored-block recursion: complex64 (default), double-float or complex128")
     ap.add_argument("--kubo-moments", type=int, default=0,
                     help="override M of the Kubo leg (small profiling case; not the benchmark)")
     ap.add_argument("--kubo-budget-gb", type=float, default=0.0,

@@ -144,11 +144,11 @@ def test_mu_nm_dd_recursion(gpu, which):
     g = orc.kernel_seq(orc.K_LORENTZ, 32, 6.0)
     if which == "bastin":
         mu = tb.kubo_mu(Ht, None, None, v_x, v_y, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True, recursion="dd")
-        mu64 = tb.kubo_mu(Ht, None, None, v_x, v_y, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True)
+        mu64 = tb.kubo_mu(Ht, None, None, v_x, v_y, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True, recursion="fp64")
         ref = orc.kubo_mu(n, cp, ri, v, 32, kets, AR=ovx, BR=ovy, g=g)
     else:
         mu = tb.kubo_mu(Ht, v_x, v_x, None, None, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True, recursion="dd")
-        mu64 = tb.kubo_mu(Ht, v_x, v_x, None, None, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True)
+        mu64 = tb.kubo_mu(Ht, v_x, v_x, None, None, M=32, kets=kets, kernel=tb.Lorentz(6.0), tensor=True, recursion="fp64")
         ref = orc.kubo_mu(n, cp, ri, v, 32, kets, AL=ovx, BL=ovx, g=g)
     assert _rel(mu, ref) <= MU_TOL, _rel(mu, ref)
     # the blocks are rounded to complex64 either way: dd and FP64 recursions agree to that rounding

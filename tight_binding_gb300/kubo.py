@@ -28,11 +28,13 @@ _RECURSION = {"fp64": 0, "mixed": capi.MU_MIXED_RECURSION, "dd": capi.MU_DD_RECU
 
 def kubo_mu(Ht: SparseMatrix, AL=None, BL=None, AR=None, BR=None, M: int = 64, R: int = 4, seed: int = 0,
             kets=None, kernel: Kernel | None = None, tensor: bool = False, budget_gb: float = 0.0,
-            recursion: str = "dd", fuse_ops: bool = False, both_sides: bool = False,
+            recursion: str = "mixed", fuse_ops: bool = False, both_sides: bool = False,
             fp64_blocks: bool = False) -> np.ndarray:
     """mu_mn = sum conj(g_m AL T_m BL r) (g_n AR T_n BR r); operators None = identity.
-    recursion: "dd" (default; double-float work blocks: FP64-class accuracy on the
-    FP32 pipe), "fp64" (complex128) or "mixed" (complex64, FP32 H~).  fuse_ops:
+    recursion: "mixed" (default: complex64 work blocks, FP32 H~; the stored
+    blocks are complex64 either way, and against the FP64 reference form the
+    sigma errors are the same as with the wider recursions), "dd" (double-float
+    work blocks: FP64-class recursion on the FP32 pipe) or "fp64" (complex128).  fuse_ops:
     form AL / AR products inside the recursion step when they share H~'s
     sparsity (same stored bits, one pass instead of two; opt-in, measured no
     faster); both_sides (with fuse_ops): run the two sides as one recursion of
@@ -108,7 +110,7 @@ def bastin_integrate(eps, zeta):
 
 def conductivity_Kubo_Bastin(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMatrix, N: int, E_min: float,
                              E_max: float, Volume: float = 1.0, R: int = 4, seed: int = 0, kernel: Kernel | None = None,
-                             tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd", fuse_ops: bool = False,
+                             tensor: bool = False, budget_gb: float = 0.0, recursion: str = "mixed", fuse_ops: bool = False,
                              velocity=None, fp64_blocks: bool = False):
     """TB/snippets.h:306-456: G(N, H, E_min-1e-8, E_max+1e-8); v = X H~ - H~ X;
     aL = g T r, aR = g v_x T v_y r; zeta at the N Chebyshev nodes; cumulative
@@ -133,7 +135,7 @@ def conductivity_Kubo_Bastin(H_og: SparseMatrix, op_x: SparseMatrix, op_y: Spars
 
 def conductivity_spectrum(H_og: SparseMatrix, op_x: SparseMatrix, op_y: SparseMatrix, N: int, R: int = 128,
                           seed: int = 0, kernel: Kernel | None = None, E_min: float = -4.0001, E_max: float = 4.0001,
-                          tensor: bool = False, budget_gb: float = 0.0, recursion: str = "dd", fuse_ops: bool = False,
+                          tensor: bool = False, budget_gb: float = 0.0, recursion: str = "mixed", fuse_ops: bool = False,
                           fp64_blocks: bool = False):
     """Kubo-Greenwood spectrum, TB/snippets.h:225-304: aR = g T r, aL = g v_x T v_x r,
     sigma(eps_k) = -<phi_L|phi_R> w(eps_k)^2 / R at the N Chebyshev nodes."""
