@@ -399,6 +399,7 @@ struct tbk_kpm_s {
   bool use_cls = false;             // one-pass kernel in the class form (translation-invariant H~)
   int pf_dist = 1;                  // L2 prefetch distance of the one-pass kernel (grid-stride waves)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t tr[3] = {nullptr, nullptr, nullptr};   // TBK_TRACE: call start, after the upload, after the readback
   double last_ms = 0.0, last_bytes = 0.0;
   int32_t last_launches = 0;
   int32_t cap_steps = 0;            // partial buffer capacity (steps)
@@ -422,6 +423,16 @@ struct tbk_kpm_s {
   int small_state = 0;              // one-launch recursion: 0 undecided, 1 used, -1 not applicable
   SmallLayout slay{};
 };
+
+// TBK_TRACE=1: every host-input solve prints its phases (upload, kets load,
+// recursion, reduction and readback) in device milliseconds to stderr
+static bool trace_on() {
+  static const bool on = [] {
+    const char* e = getenv("TBK_TRACE");
+    return e && atoi(e) != 0;
+  }();
+  return on;
+}
 
 // single-chunk plans whose work blocks fit in 64 MiB are launch-bound: replay
 // their recursion as a graph
@@ -804,7 +815,17 @@ static int kpm_run_impl(tbk_kpm_s* P, int32_t n_mom, bool braket, KL&& kets_load
   else TBK_CUDA(cudaMemcpyAsync(mu_out, P->mu.p, sizeof(double) * n_mom, cudaMemcpyDeviceToHost, st));
   int herr = 0;
   TBK_CUDA(cudaMemcpyAsync(&herr, P->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (P->tr[2]) TBK_CUDA(cudaEventRecord(P->tr[2], st));
   TBK_CUDA(cudaStreamSynchronize(st));
+  if (P->tr[2] && P->n_chunks == 1) {
+    float up = 0.f, ld = 0.f, rec = 0.f, tail = 0.f;
+    cudaEventElapsedTime(&up, P->tr[0], P->tr[1]);
+    cudaEventElapsedTime(&ld, P->tr[1], P->ev0);
+    cudaEventElapsedTime(&rec, P->ev0, P->ev1);
+    cudaEventElapsedTime(&tail, P->ev1, P->tr[2]);
+    fprintf(stderr, "tbk trace: upload %.3f ms, kets load %.3f ms, recursion %.3f ms, reduce+readback %.3f ms\n", up,
+            ld, rec, tail);
+  }
   if (herr) return fail(TBK_ERR_TIMEOUT, "recursion kernel gave up waiting (code %d)", herr);
   // algorithmic DRAM bytes per recursion launch (average over the launches)
   const double vec = (double)P->n * P->Rc * P->csize;
@@ -937,6 +958,8 @@ void tbk_kpm_destroy(tbk_kpm P) {
   cudaDeviceSynchronize();
   if (P->ev0) cudaEventDestroy(P->ev0);
   if (P->ev1) cudaEventDestroy(P->ev1);
+  for (auto e : P->tr)
+    if (e) cudaEventDestroy(e);
   if (P->gexec) cudaGraphExecDestroy(P->gexec);
   if (P->cap_st) cudaStreamDestroy(P->cap_st);
   delete P;
@@ -957,6 +980,9 @@ int tbk_kpm_run(tbk_kpm P, int32_t n_mom, const double* bras, const double* kets
   if (!dev) {
     const size_t need = same ? in_bytes : 2 * in_bytes;
     if (P->stage.bytes < need) TBK_TRY(P->stage.alloc(need));
+    if (trace_on() && !P->tr[0])
+      for (auto& e : P->tr) TBK_CUDA(cudaEventCreate(&e));
+    if (P->tr[0]) TBK_CUDA(cudaEventRecord(P->tr[0], st));
     TBK_CUDA(cudaMemcpyAsync(P->stage.p, kets, in_bytes, cudaMemcpyHostToDevice, st));
     kets_dev = P->stage.as<double2>();
     bras_dev = kets_dev;
@@ -964,6 +990,7 @@ int tbk_kpm_run(tbk_kpm P, int32_t n_mom, const double* bras, const double* kets
       TBK_CUDA(cudaMemcpyAsync(P->stage.as<char>() + in_bytes, bras, in_bytes, cudaMemcpyHostToDevice, st));
       bras_dev = reinterpret_cast<const double2*>(P->stage.as<char>() + in_bytes);
     }
+    if (P->tr[1]) TBK_CUDA(cudaEventRecord(P->tr[1], st));
   }
   const bool mixed = P->prec == TBK_PREC_MIXED;
   auto load_from = [&](const double2* src) {
