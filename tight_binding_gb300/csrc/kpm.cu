@@ -434,6 +434,27 @@ static bool trace_on() {
   return on;
 }
 
+// Device view of a host pointer when it lies in pinned (registered) host
+// memory, else null.
+static const double2* mapped_host(const double* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type == cudaMemoryTypeHost && at.devicePointer) return static_cast<const double2*>(at.devicePointer);
+  return nullptr;
+}
+// TBK_STAGE_UPLOAD=1: copy host inputs into a device staging buffer even when
+// they are pinned (A/B of the in-place read)
+static bool stage_uploads() {
+  static const bool on = [] {
+    const char* e = getenv("TBK_STAGE_UPLOAD");
+    return e && atoi(e) != 0;
+  }();
+  return on;
+}
+
 // single-chunk plans whose work blocks fit in 64 MiB are launch-bound: replay
 // their recursion as a graph
 constexpr size_t kGraphBlockBytes = 64u << 20;
@@ -974,10 +995,30 @@ int tbk_kpm_run(tbk_kpm P, int32_t n_mom, const double* bras, const double* kets
   if (doubling && bras != kets) return fail(TBK_ERR_INVALID, "TBK_FLAG_DOUBLING needs bras == kets");
   const bool same = bras == kets;
   const size_t in_bytes = sizeof(double2) * (size_t)P->n * P->R;
-  // host inputs: one H2D copy each into staging; every chunk transposes its columns from there
+  // Host inputs.  Pinned (page-locked, registered) host memory is mapped into
+  // the device's address space: the load kernel then reads its columns in
+  // place over the host link (NVLink-C2C on GB300), with no staging buffer and
+  // no separate copy.  Other host memory is copied into a device staging
+  // buffer first (one copy each); every chunk transposes its columns from there.
   const double2* kets_dev = reinterpret_cast<const double2*>(kets);
   const double2* bras_dev = reinterpret_cast<const double2*>(bras);
-  if (!dev) {
+  bool mapped = false;
+  if (!dev && !stage_uploads()) {
+    const double2* km = mapped_host(kets);
+    const double2* bm = same ? km : mapped_host(bras);
+    if (km && bm) {
+      kets_dev = km;
+      bras_dev = bm;
+      mapped = true;
+      if (trace_on() && !P->tr[0])
+        for (auto& e : P->tr) TBK_CUDA(cudaEventCreate(&e));
+      if (P->tr[0]) {
+        TBK_CUDA(cudaEventRecord(P->tr[0], st));
+        TBK_CUDA(cudaEventRecord(P->tr[1], st));
+      }
+    }
+  }
+  if (!dev && !mapped) {
     const size_t need = same ? in_bytes : 2 * in_bytes;
     if (P->stage.bytes < need) TBK_TRY(P->stage.alloc(need));
     if (trace_on() && !P->tr[0])

@@ -24,6 +24,7 @@
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -79,7 +80,15 @@ __host__ __device__ constexpr int srv_rows_per_warp(int cs, int R) { return 32 /
 // Rows per slab: eight warp iterations, 4 KB of v_s.  The slab is the unit of
 // one moment partial, so this fixes the summation order; it depends on (cs, R)
 // alone.
-inline int srv_slab_rows(int cs, int R, int64_t) { return srv_rows_per_warp(cs, R) * kIterPerSlab; }
+inline int srv_iters_per_slab() {
+  static const int it = [] {
+    const char* e = getenv("TBK_SERVE_SLAB_ITERS");             // tuning override
+    const int v = e ? atoi(e) : 0;
+    return v >= 1 && v <= 256 ? v : kIterPerSlab;
+  }();
+  return it;
+}
+inline int srv_slab_rows(int cs, int R, int64_t) { return srv_rows_per_warp(cs, R) * srv_iters_per_slab(); }
 
 // One doubling recursion step (step j of the round) over the slabs of group g,
 // one warp per slab (no barriers: warps run independently).  The six pointers
