@@ -689,11 +689,12 @@ def serve_line(args):
 def run_serve_single(args):
     """Profiling case of the serving step kernel: one honeycomb --cells^2 request
     (t = 1, disorder W = 1 seed 1, R = 32, M = --moments, mixed) through a server
-    with the launch-shape tuner off, twice; reports the second's HBM rate."""
+    (launch-shape tuner on unless --serve-no-tune), twice; reports the second's
+    HBM rate."""
     import tight_binding_gb300 as tb
     from tight_binding_gb300.serving import model_bounds, model_cell
 
-    srv = tb.DosServer(autotune=False)
+    srv = tb.DosServer(autotune=not args.serve_no_tune)
     X = tb.PartialLattice(model_cell("honeycomb"), (args.cells, args.cells))
     X.set_scalar_disorder(1.0, 1)
     lo, hi = model_bounds("honeycomb", 1.0)
@@ -909,6 +910,7 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=120.0)
     ap.add_argument("--serve-round", type=int, default=16)
     ap.add_argument("--serve-step-gb", type=float, default=2.0)
+    ap.add_argument("--serve-no-tune", action="store_true", help="serving profiling case without the tuner")
     ap.add_argument("--serve-single", action="store_true",
                     help="one honeycomb --cells^2 request through the server (profiling case)")
     ap.add_argument("--gemm", type=int, nargs=2, metavar=("M", "K"),

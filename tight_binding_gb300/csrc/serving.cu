@@ -1134,7 +1134,9 @@ void loop_main(tbk_server_s* S) {
 }
 
 // Times each candidate launch shape of every real group on a synthetic width-4
-// operator of ~64 MB per vector block (TBK_SERVE_TUNE_MB overrides) and keeps
+// operator of ~256 MB per vector block — two blocks exceed the 129 MB L2, as
+// the requests that dominate the traffic do, so that the L2 prefetch distance
+// is chosen on DRAM streams (TBK_SERVE_TUNE_MB overrides) — and keeps
 // the fastest (grid, prefetch distance).  Each width is tuned twice: through
 // the synthetic ELL, and in the class form with the same couplings as one
 // class (offsets +-1, +-257, clamped at the ends of the block); the complex-H
@@ -1148,7 +1150,7 @@ int autotune(tbk_server_s* S) {
   for (int prec = 0; prec < 3 && rc_all == TBK_OK; ++prec) {
     for (int rc = 4; rc <= (prec == TBK_PREC_MIXED ? 64 : 32) && rc_all == TBK_OK; rc <<= 1) {
       const int cs = prec == TBK_PREC_MIXED ? 8 : 16;
-      int64_t tune_mb = 64;
+      int64_t tune_mb = 256;
       if (const char* ev = getenv("TBK_SERVE_TUNE_MB")) tune_mb = std::max(1, atoi(ev));   // tuning override
       int32_t n = (int32_t)((tune_mb << 20) / ((int64_t)rc * cs));
       const int sr = srv_slab_rows(cs, rc, n);
