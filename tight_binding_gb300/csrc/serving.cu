@@ -102,10 +102,10 @@ inline int srv_slab_rows(int cs, int R, int64_t) { return srv_rows_per_warp(cs, 
 // which are the step sums of the doubling identities mu_2s = 2<v_s|v_s> - mu_0,
 // mu_2s-1 = 2<v_s|v_s-1> - mu_1.
 // CLS (a group of requests whose H~ has row classes): neighbours are row +
-// offset from the request's class table (read through L1), the row's class
-// byte is loaded one warp iteration ahead; no column index or value stream.
+// offset from the request's class table (read through L1); no column index or
+// value stream.
 template <typename F, int R, bool CPLX_H, bool CLS>
-__global__ void __launch_bounds__(kSrvThreads, (sizeof(F) == 4 && !CLS) ? 5 : 4) srv_step_kernel(
+__global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_kernel(
     const SHdr* __restrict__ hdr, const SLane* __restrict__ lanes, const SSlab* __restrict__ slabs, int32_t g,
     int32_t j, int32_t reverse, int32_t pf_dist, double* __restrict__ part, int32_t slab_cap) {
   using CT = typename C2<F>::T;
@@ -171,16 +171,9 @@ __global__ void __launch_bounds__(kSrvThreads, (sizeof(F) == 4 && !CLS) ? 5 : 4)
     const bool dot_only = s == ns - 1 && s > 0;
     const int32_t rend = min(sl.row0 + slab_rows, n);
     F m0 = 0, m1 = 0;
-    uint32_t c_next = 0;                       // class form: class of this lane's next row
-    if constexpr (CLS) {
-      const int32_t r0 = sl.row0 + lane / LPR;
-      if (r0 < rend) c_next = __ldg(my->cls + r0);
-    }
     for (int32_t rb = sl.row0; rb < rend; rb += RPW) {
       const int32_t r = rb + lane / LPR;
       if (r >= rend) break;
-      const uint32_t c_cur = c_next;
-      if constexpr (CLS) c_next = r + RPW < rend ? __ldg(my->cls + r + RPW) : 0u;
       const int64_t me = (int64_t)r * LPR + sub;
       const LaneV<F, VPL> xs = ld_ro<F, VPL>(my->x + me * VPL);
       LaneV<F, VPL> prev;
@@ -195,12 +188,12 @@ __global__ void __launch_bounds__(kSrvThreads, (sizeof(F) == 4 && !CLS) ? 5 : 4)
       for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
       if (!dot_only && CLS) {
         HVal<F, CPLX_H>::load(my->diag, r).template fma<VPL>(xs, acc);
-        const int32_t cw = my->cw;
-        const int32_t tb = (int32_t)c_cur * cw;
-        const int32_t cnt = __ldg(my->soff + c_cur);
-        const int32_t* co = my->ecol;
-        const F* cv = my->eval;
-        const CT* xp = my->x;
+        // the row's class, then its entry count and table row; the lane's
+        // pointers are re-read from the warp's shared slot at each use (as the
+        // ELL path does) to keep the kernel at five CTAs per SM
+        const uint32_t cr = __ldg(my->cls + r);
+        const int32_t tb = (int32_t)cr * my->cw;
+        const int32_t cnt = __ldg(my->soff + cr);
         for (int k = 0; k < cnt; k += 4) {
           HVal<F, CPLX_H> h[4];
           LaneV<F, VPL> xv[4];
@@ -209,9 +202,9 @@ __global__ void __launch_bounds__(kSrvThreads, (sizeof(F) == 4 && !CLS) ? 5 : 4)
             const bool v = k + u < cnt;
             // rows are verified equal to their class: r + offset is the row's
             // column; the clamp only keeps a bad table inside the block
-            const int32_t c = v ? min(max(r + __ldg(co + tb + k + u), 0), n - 1) : r;
-            h[u] = v ? HVal<F, CPLX_H>::load(cv, tb + k + u) : HVal<F, CPLX_H>::zero();
-            xv[u] = v ? ld_ro<F, VPL>(xp + ((int64_t)c * LPR + sub) * VPL) : xs;
+            const int32_t c = v ? min(max(r + __ldg(my->ecol + tb + k + u), 0), n - 1) : r;
+            h[u] = v ? HVal<F, CPLX_H>::load(my->eval, tb + k + u) : HVal<F, CPLX_H>::zero();
+            xv[u] = v ? ld_ro<F, VPL>(my->x + ((int64_t)c * LPR + sub) * VPL) : xs;
           }
 #pragma unroll
           for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
