@@ -171,9 +171,16 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
     const bool dot_only = s == ns - 1 && s > 0;
     const int32_t rend = min(sl.row0 + slab_rows, n);
     F m0 = 0, m1 = 0;
+    uint32_t c_next = 0;                       // class form: class of this lane's next row
+    if constexpr (CLS) {
+      const int32_t r0 = sl.row0 + lane / LPR;
+      if (r0 < rend) c_next = __ldg(my->cls + r0);
+    }
     for (int32_t rb = sl.row0; rb < rend; rb += RPW) {
       const int32_t r = rb + lane / LPR;
       if (r >= rend) break;
+      const uint32_t cr = c_next;
+      if constexpr (CLS) c_next = r + RPW < rend ? __ldg(my->cls + r + RPW) : 0u;
       const int64_t me = (int64_t)r * LPR + sub;
       const LaneV<F, VPL> xs = ld_ro<F, VPL>(my->x + me * VPL);
       LaneV<F, VPL> prev;
@@ -188,10 +195,9 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
       for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
       if (!dot_only && CLS) {
         HVal<F, CPLX_H>::load(my->diag, r).template fma<VPL>(xs, acc);
-        // the row's class, then its entry count and table row; the lane's
-        // pointers are re-read from the warp's shared slot at each use (as the
-        // ELL path does) to keep the kernel at five CTAs per SM
-        const uint32_t cr = __ldg(my->cls + r);
+        // the row's class (loaded one warp iteration ahead), its entry count
+        // and table row; the lane's pointers are re-read from the warp's shared
+        // slot at each use (as the ELL path does) to keep registers down
         const int32_t tb = (int32_t)cr * my->cw;
         const int32_t cnt = __ldg(my->soff + cr);
         for (int k = 0; k < cnt; k += 4) {
