@@ -106,6 +106,30 @@ def test_alone_equals_in_mix(gpu, prec):
     assert np.array_equal(alone, other)
 
 
+def test_class_form_opt_in(gpu, monkeypatch):
+    """TBK_SERVE_CLASSES=1 (read when a server is created) runs requests whose
+    H~ has row classes through the class-form kernels: the same bits as the
+    default ELL form, alone and in a mix."""
+    tb = gpu
+    cells = {k: cell(tb, k) for k in ("square", "honeycomb", "kagome", "lieb", "fcc")}
+    probe = dict(kind="honeycomb", L=48, W=1.3, M=200, R=16, prec="mixed", seed=77)
+    with tb.DosServer(autotune=False) as srv:
+        ell, _ = srv.result(_submit(tb, srv, probe, cells))
+    monkeypatch.setenv("TBK_SERVE_CLASSES", "1")
+    with tb.DosServer(autotune=True, steps_per_round=16) as srv:
+        alone, _ = srv.result(_submit(tb, srv, probe, cells))
+        mix = _mix(tb, cells)
+        tickets = [_submit(tb, srv, c, cells) for c in mix[:6]]
+        t_probe = _submit(tb, srv, probe, cells)
+        tickets += [_submit(tb, srv, c, cells) for c in mix[6:]]
+        in_mix, _ = srv.result(t_probe)
+        for t in tickets:
+            srv.result(t)
+        assert sum(t["form"] == "classes" for t in srv.tuning()) == 13
+    assert np.array_equal(alone, in_mix)
+    assert np.array_equal(alone, ell)
+
+
 def test_budget_admission(gpu):
     tb = gpu
     X = lattice(tb, "square", 96, 1.0, seed=1)

@@ -201,6 +201,9 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
         const int32_t tb = (int32_t)cr * my->cw;
         const int32_t cnt = __ldg(my->soff + cr);
         for (int k = 0; k < cnt; k += 4) {
+          const int32_t* co = my->ecol + tb + k;           // once per group of 4, as the ELL path
+          const F* cv = my->eval;
+          const CT* xp = my->x;
           HVal<F, CPLX_H> h[4];
           LaneV<F, VPL> xv[4];
 #pragma unroll
@@ -208,9 +211,9 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
             const bool v = k + u < cnt;
             // rows are verified equal to their class: r + offset is the row's
             // column; the clamp only keeps a bad table inside the block
-            const int32_t c = v ? min(max(r + __ldg(my->ecol + tb + k + u), 0), n - 1) : r;
-            h[u] = v ? HVal<F, CPLX_H>::load(my->eval, tb + k + u) : HVal<F, CPLX_H>::zero();
-            xv[u] = v ? ld_ro<F, VPL>(my->x + ((int64_t)c * LPR + sub) * VPL) : xs;
+            const int32_t c = v ? min(max(r + __ldg(co + u), 0), n - 1) : r;
+            h[u] = v ? HVal<F, CPLX_H>::load(cv, tb + k + u) : HVal<F, CPLX_H>::zero();
+            xv[u] = v ? ld_ro<F, VPL>(xp + ((int64_t)c * LPR + sub) * VPL) : xs;
           }
 #pragma unroll
           for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
@@ -598,6 +601,9 @@ struct tbk_server_s {
   int dev = 0;
   int sms = 152;
   int S = 16;
+  // class form for requests whose H~ has row classes (TBK_SERVE_CLASSES=1 at
+  // create): measured no faster than the ELL form in this kernel, so opt-in
+  bool classes = false;
   double budget = 120e9, step_budget = 2e9;
   int max_resident = 4096;
   cudaStream_t st_loop = nullptr, st_admit = nullptr;
@@ -685,7 +691,7 @@ int build_request(tbk_server_s* S, SrvRequest* r) {
   Ht->col_ptr.release();
   Ht->row_idx.release();
   Ht->values.release();
-  TBK_TRY(ensure_classes(Ht, st));
+  if (S->classes) TBK_TRY(ensure_classes(Ht, st));
   const bool mixed = q.precision == TBK_PREC_MIXED;
   const bool cls = Ht->ell.cls_state == 1;
   if (q.precision == TBK_PREC_DD) TBK_TRY(ensure_ell_dd(Ht, st));
@@ -1003,7 +1009,7 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
     for (int32_t c = 0; c < r->n_lanes; ++c) {
       SLane& L = lanes[li];
       const int pq = r->q.precision;
-      if (E.cls_state == 1) {
+      if (code_cls(r->code)) {
         L.soff = E.cls_cnt.as<int32_t>();
         L.ecol = E.cls_off.as<int32_t>();
         L.eval = pq == TBK_PREC_MIXED ? E.cls_v32.p : pq == TBK_PREC_DD ? E.cls_vdd.p : E.cls_v64.p;
@@ -1316,6 +1322,7 @@ int tbk_server_create(tbk_server* out, const tbk_server_config* cfg) {
     return fail(TBK_ERR_CUDA, "tbk_server_create: no CUDA device");
   }
   auto* S = new tbk_server_s();
+  if (const char* e = getenv("TBK_SERVE_CLASSES")) S->classes = atoi(e) != 0;
   S->epoch = Clock::now();
   if (cfg) {
     if (cfg->budget_gb > 0) S->budget = cfg->budget_gb * 1e9;
