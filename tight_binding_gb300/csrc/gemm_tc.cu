@@ -168,10 +168,14 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
       "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
       : "memory");
 }
+// TF32 value of x, rounded to nearest with ties away from zero (the rounding
+// of cvt.rna.tf32.f32), on the integer pipe: TF32 keeps 10 of FP32's 23
+// mantissa bits, so adding half a unit of the 13 dropped bits (0x1000) to the
+// sign-magnitude pattern and clearing them rounds the magnitude half-up
+// (a carry into the exponent is the correct rounding to the next binade).
+// Finite inputs only (the stored blocks are finite).
 __device__ __forceinline__ float to_tf32_rna(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 // (hi, lo) += v with TwoSum (Knuth): hi + lo carries the sum to ~2^-48.
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
