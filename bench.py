@@ -425,10 +425,11 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sites": int(N), "nnz_Ht": int(Ht.nnz), "moments": M_MOM,
-                   "vectors": R_VEC, "energies": N_E, "precision": "complex64 recursion, FP64 moment sums, doubling",
-                   "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (537 MB vector block per step, 129 MB L2); no flush"},
+        "config": {"workload": WORKLOAD, "sites": int(N), "moments": M_MOM, "vectors": R_VEC},
+        "config_details": {"nnz_Ht": int(Ht.nnz), "energies": N_E,
+                           "precision": "complex64 recursion, FP64 moment sums, doubling",
+                           "parallelism": "replicas" if ws > 1 else "single GPU",
+                           "l2": "inputs larger than L2 (537 MB vector block per step, 129 MB L2); no flush"},
         "latency_ms": {"p50": float(np.percentile(per_step, 50)), "p99": float(np.percentile(per_step, 99))},
         "e2e": e2e, "gpu_launches": launches_per_step * args.steps,
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
