@@ -11,12 +11,17 @@ moment sums and Chebyshev doubling (bras = kets), Jackson kernel, rho(E) on
 metric: site-moment-vector updates/s = N * M * R / step time.
   value : inputs resident in HBM (H~ and the kets block), device-timed.
   e2e   : the same solve through the C ABI drop-in (tbk_cheb_braket_real) with
-          pinned HOST buffers: H~ CSC + kets uploaded and moments read back
-          inside the timed region.
+          pinned HOST buffers: H~ CSC uploaded and compared with the cached
+          plan's, kets read from host memory, moments read back, all inside
+          the timed region of every call.
 Also measured in the same run: the plain FP64 GPU path (complex128, one
-moment per step, bras read every step — the reference's algorithm, fused) and
-the CPU oracle (the reference's CPU recursion restated in C, OpenMP over the
-random vectors) on a bounded sample.
+moment per step, bras read every step — the reference's algorithm, fused),
+the double-float plain path, the reference's own GPU algorithm (cuSPARSE
+SpMM + cuBLAS dot per moment, restated in baseline/cusparse_kpm.cu), the CPU
+oracle (the reference's CPU recursion restated in C, OpenMP over the random
+vectors) on a bounded sample, full-size parity (all moments and rho against
+the complex128 recursion), and one sub-record per other configuration
+(`configs`: 1, 3, 5 and a shortened 4).
 
 --impl reference: times the CPU restatement of the reference's KPM loop
 (TB/numerical.h:363-381) on all host cores, on a bounded sample of the same
