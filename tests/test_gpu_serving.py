@@ -106,16 +106,17 @@ def test_alone_equals_in_mix(gpu, prec):
     assert np.array_equal(alone, other)
 
 
-def test_class_form_opt_in(gpu, monkeypatch):
-    """TBK_SERVE_CLASSES=1 (read when a server is created) runs requests whose
-    H~ has row classes through the class-form kernels: the same bits as the
-    default ELL form, alone and in a mix."""
+def test_class_form_equals_ell(gpu, monkeypatch):
+    """Requests whose H~ has row classes run in the class form by default; a
+    server created with TBK_SERVE_CLASSES=0 keeps them in the ELL form.  Both
+    give the same bits, alone and in a mix."""
     tb = gpu
     cells = {k: cell(tb, k) for k in ("square", "honeycomb", "kagome", "lieb", "fcc")}
     probe = dict(kind="honeycomb", L=48, W=1.3, M=200, R=16, prec="mixed", seed=77)
+    monkeypatch.setenv("TBK_SERVE_CLASSES", "0")
     with tb.DosServer(autotune=False) as srv:
         ell, _ = srv.result(_submit(tb, srv, probe, cells))
-    monkeypatch.setenv("TBK_SERVE_CLASSES", "1")
+    monkeypatch.delenv("TBK_SERVE_CLASSES")
     with tb.DosServer(autotune=True, steps_per_round=16) as srv:
         alone, _ = srv.result(_submit(tb, srv, probe, cells))
         mix = _mix(tb, cells)

@@ -17,8 +17,9 @@
 //     written straight into pinned host memory.  Graphs are cached per group
 //     set; what changes from round to round (which requests, at which step)
 //     lives in a device table copied in before the launch.
-// Each slab (a fixed number of a request's rows) is one CTA's work and one
-// partial; the slab partials of a request are summed in slab order.  So a
+// A request's rows are cut into tiles (one CTA's work) of kSrvWarps slabs;
+// each slab (a fixed set of the tile's rows) is one warp's work and one moment
+// partial, and the slab partials of a request are summed in slab order.  So a
 // request's moments depend only on the request, never on what runs beside it.
 #include <algorithm>
 #include <atomic>
@@ -59,8 +60,9 @@ struct SLane {                      // up to 64 vectors of one request (device v
   void* vb;                         // v_s for odd s
   int32_t n, n_steps, s0, req;
   int32_t slab_begin, n_slabs, slab_rows, cls_w;   // cls_w: class form, entries per class
+  int32_t n_cls, pad;               // class form: classes
 };
-struct SSlab {
+struct STile {                      // kSrvWarps slabs of one lane, from row row0
   int32_t lane, row0;
 };
 struct SReq {
@@ -71,15 +73,15 @@ struct SReq {
 struct SHdr {
   int32_t grp_begin[kGroups];
   int32_t grp_count[kGroups];
-  int32_t n_lanes, n_slabs, n_reqs, pad;
+  int32_t n_lanes, n_tiles, n_reqs, pad;
 };
 
 // complex element size cs = 8 (complex64) or 16 (complex128); width R
 __host__ __device__ constexpr int srv_vpl(int cs, int R) { return (cs == 8 && R >= 2) ? 2 : 1; }
 __host__ __device__ constexpr int srv_rows_per_warp(int cs, int R) { return 32 / (R / srv_vpl(cs, R)); }
-// Rows per slab: eight warp iterations, 4 KB of v_s.  The slab is the unit of
-// one moment partial, so this fixes the summation order; it depends on (cs, R)
-// alone.
+// Rows per slab: eight warp iterations, 4 KB of v_s (a tile: kSrvWarps slabs).
+// The slab is the unit of one moment partial, so this fixes the summation
+// order; it depends on (cs, R) alone.
 inline int srv_iters_per_slab() {
   static const int it = [] {
     const char* e = getenv("TBK_SERVE_SLAB_ITERS");             // tuning override
@@ -90,36 +92,46 @@ inline int srv_iters_per_slab() {
 }
 inline int srv_slab_rows(int cs, int R, int64_t) { return srv_rows_per_warp(cs, R) * srv_iters_per_slab(); }
 
-// One doubling recursion step (step j of the round) over the slabs of group g,
-// one warp per slab (no barriers: warps run independently).  The six pointers
-// of the slab's lane live in a per-warp shared-memory slot read at each use, so
-// that they hold no registers across the gathers: complex64 groups fit 5 CTAs
-// per SM (wider types keep 4).  With s = s0 + j
-// the lane's step, x = v_s and y = v_{s-1} on entry:
+// One doubling recursion step (step j of the round) over the tiles of group g.
+// A lane's rows are cut into tiles of kSrvWarps slabs (kSrvWarps * slab_rows
+// rows); a CTA takes a tile, and warp w's slab is the tile's row groups w,
+// w + kSrvWarps, w + 2 kSrvWarps, ... (RPW rows each), so that at each warp
+// iteration the CTA's warps read consecutive rows (whole DRAM pages) together.
+// A slab is one moment partial: one warp's per-lane sums over its rows, then a
+// fixed shuffle tree; slab w of the lane's k-th tile is partial k kSrvWarps + w.
+// With s = s0 + j the lane's step, x = v_s and y = v_{s-1} on entry:
 //   s == 0:         y = H x,             partials <x|x>, <x|y>
 //   0 < s < last:   y = 2 H x - y,       partials <x|x>, <x|y_in>
 //   s == last:      no product, no store, partials <x|x>, <x|y_in>
 // which are the step sums of the doubling identities mu_2s = 2<v_s|v_s> - mu_0,
 // mu_2s-1 = 2<v_s|v_s-1> - mu_1.
-// CLS (a group of requests whose H~ has row classes): neighbours are row +
-// offset from the request's class table (read through L1); no column index or
-// value stream.
+// The lane's pointers live in a per-CTA shared slot, re-read at each use so
+// that they hold no registers across the gathers (complex64 groups fit 6 CTAs
+// per SM in the class form, 5 in the ELL form, wider types 4); a CTA reloads
+// the slot only when its next tile belongs to another lane.
+// CLS (groups whose H~ has row classes): the slot also holds the lane's class
+// table (entry counts, column offsets, values), where the streamed vector rows
+// cannot evict it; a row's neighbours are row + offset, its values come from
+// the table, and the only index it loads (its class byte) is issued one warp
+// iteration ahead.  Same entries in the same order as the ELL: the same sums.
 template <typename F, int R, bool CPLX_H, bool CLS>
-__global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_kernel(
-    const SHdr* __restrict__ hdr, const SLane* __restrict__ lanes, const SSlab* __restrict__ slabs, int32_t g,
+__global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? (CLS ? 6 : 5) : 4) srv_step_kernel(
+    const SHdr* __restrict__ hdr, const SLane* __restrict__ lanes, const STile* __restrict__ tiles, int32_t g,
     int32_t j, int32_t reverse, int32_t pf_dist, double* __restrict__ part, int32_t slab_cap) {
   using CT = typename C2<F>::T;
   constexpr int CS = (int)sizeof(CT);
   constexpr int VPL = srv_vpl(CS, R);
   constexpr int LPR = R / VPL;
   constexpr int RPW = 32 / LPR;
+  constexpr int STRIDE = RPW * kSrvWarps;                      // rows per CTA warp iteration
   static_assert(LPR >= 1 && LPR <= 32 && (32 % LPR) == 0, "width out of range");
-
-  const int lane = threadIdx.x & 31;
-  const int sub = lane % LPR;
-  const int32_t begin = hdr->grp_begin[g], cnt = hdr->grp_count[g];
-  const int32_t nw = (int32_t)gridDim.x * kSrvWarps;
-  struct WP {
+  constexpr int VW = (CPLX_H ? 2 : 1) * (int)sizeof(F) / 4;    // 4-byte words per class-table value
+  // class table: values, then offsets, then counts, at fixed word offsets
+  __shared__ __align__(16) uint32_t tab[CLS ? kMaxClassEntries * (VW + 1) + kMaxClasses : 1];
+  const F* s_val = reinterpret_cast<const F*>(tab);
+  const int32_t* s_off = reinterpret_cast<const int32_t*>(tab + kMaxClassEntries * VW);
+  const int32_t* s_cnt = reinterpret_cast<const int32_t*>(tab + kMaxClassEntries * (VW + 1));
+  struct TP {
     const CT* x;
     CT* y;
     const int32_t* soff;
@@ -127,24 +139,56 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
     const F* eval;
     const F* diag;
     const uint8_t* cls;
-    int32_t cw;
+    int32_t n, w, s, ns, rows;
   };
-  __shared__ WP wp[kSrvWarps];
-  volatile WP* my = wp + (threadIdx.x >> 5);
-  for (int32_t t = (int32_t)blockIdx.x * kSrvWarps + (threadIdx.x >> 5); t < cnt; t += nw) {
-    const int32_t i = reverse ? cnt - 1 - t : t;
-    const SSlab sl = slabs[begin + i];
-    const SLane* L = lanes + sl.lane;
-    const int32_t n = L->n, ns = L->n_steps, s = L->s0 + j, slab_rows = L->slab_rows;
-    if (s >= ns) continue;
-    if (pf_dist > 0 && lane == 0) {
-      // the slab this warp reaches pf_dist iterations later: v_s, v_{s-1} rows into L2
-      const int32_t tf = t + pf_dist * nw;
+  __shared__ TP tp;
+  volatile TP* vt = &tp;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane % LPR;
+  const int32_t begin = hdr->grp_begin[g], cnt = hdr->grp_count[g];
+  int32_t cur = -1;                                            // the lane whose slot the CTA holds
+  for (int32_t t = blockIdx.x; t < cnt; t += gridDim.x) {
+    const int32_t ti = begin + (reverse ? cnt - 1 - t : t);
+    const STile tl = tiles[ti];
+    if (tl.lane != cur) {                                      // uniform over the CTA
+      __syncthreads();                                         // nobody reads the previous slot any more
+      const SLane* L = lanes + tl.lane;
+      if constexpr (CLS) {
+        const int32_t ne = L->n_cls * L->cls_w;
+        const uint32_t* gv = static_cast<const uint32_t*>(L->eval);
+        for (int32_t q = threadIdx.x; q < ne * VW; q += kSrvThreads) tab[q] = __ldg(gv + q);
+        for (int32_t q = threadIdx.x; q < ne; q += kSrvThreads)
+          tab[kMaxClassEntries * VW + q] = (uint32_t)__ldg(L->ecol + q);
+        for (int32_t q = threadIdx.x; q < L->n_cls; q += kSrvThreads)
+          tab[kMaxClassEntries * (VW + 1) + q] = (uint32_t)__ldg(L->soff + q);
+      }
+      if (threadIdx.x == 0) {
+        const int32_t sl = L->s0 + j;
+        tp.x = static_cast<const CT*>((sl & 1) ? L->vb : L->va);
+        tp.y = static_cast<CT*>((sl & 1) ? L->va : L->vb);
+        tp.soff = L->soff;
+        tp.ecol = L->ecol;
+        tp.eval = static_cast<const F*>(L->eval);
+        tp.diag = static_cast<const F*>(L->diag);
+        tp.cls = L->cls;
+        tp.n = L->n;
+        tp.w = L->cls_w;
+        tp.s = sl;
+        tp.ns = L->n_steps;
+        tp.rows = L->slab_rows * kSrvWarps;
+      }
+      __syncthreads();
+      cur = tl.lane;
+    }
+    if (pf_dist > 0 && threadIdx.x == 0) {
+      // the tile this CTA reaches pf_dist iterations later: v_s, v_{s-1} rows into L2
+      const int32_t tf = t + pf_dist * (int32_t)gridDim.x;
       if (tf < cnt) {
-        const SSlab sf = slabs[begin + (reverse ? cnt - 1 - tf : tf)];
+        const STile sf = tiles[begin + (reverse ? cnt - 1 - tf : tf)];
         const SLane* Lf = lanes + sf.lane;
         const int32_t sfs = Lf->s0 + j;
-        const int32_t nr = min(Lf->slab_rows, Lf->n - sf.row0);
+        const int32_t nr = min(Lf->slab_rows * kSrvWarps, Lf->n - sf.row0);
         if (sfs < Lf->n_steps && nr > 0) {
           const uint32_t nb = (uint32_t)nr * (uint32_t)(R * CS);
           if ((nb & 15u) == 0) {
@@ -156,36 +200,27 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
         }
       }
     }
-    if (lane == 0) {
-      my->x = static_cast<const CT*>((s & 1) ? L->vb : L->va);
-      my->y = static_cast<CT*>((s & 1) ? L->va : L->vb);
-      my->soff = L->soff;
-      my->ecol = L->ecol;
-      my->eval = static_cast<const F*>(L->eval);
-      my->diag = static_cast<const F*>(L->diag);
-      my->cls = L->cls;
-      my->cw = L->cls_w;
-    }
-    __syncwarp();
+    const int32_t s = vt->s, ns = vt->ns;
+    if (s >= ns) continue;                                     // the lane's recursion ended before this step
     const bool first = s == 0;
     const bool dot_only = s == ns - 1 && s > 0;
-    const int32_t rend = min(sl.row0 + slab_rows, n);
+    const int32_t rend = min(tl.row0 + vt->rows, vt->n);
     F m0 = 0, m1 = 0;
-    uint32_t c_next = 0;                       // class form: class of this lane's next row
+    uint32_t c_next = 0;                                       // class form: class of this lane's next row
     if constexpr (CLS) {
-      const int32_t r0 = sl.row0 + lane / LPR;
-      if (r0 < rend) c_next = __ldg(my->cls + r0);
+      const int32_t r0 = tl.row0 + warp * RPW + lane / LPR;
+      if (r0 < rend) c_next = __ldg(vt->cls + r0);
     }
-    for (int32_t rb = sl.row0; rb < rend; rb += RPW) {
+    for (int32_t rb = tl.row0 + warp * RPW; rb < rend; rb += STRIDE) {
       const int32_t r = rb + lane / LPR;
       if (r >= rend) break;
       const uint32_t cr = c_next;
-      if constexpr (CLS) c_next = r + RPW < rend ? __ldg(my->cls + r + RPW) : 0u;
+      if constexpr (CLS) c_next = r + STRIDE < rend ? __ldg(vt->cls + r + STRIDE) : 0u;
       const int64_t me = (int64_t)r * LPR + sub;
-      const LaneV<F, VPL> xs = ld_ro<F, VPL>(my->x + me * VPL);
+      const LaneV<F, VPL> xs = ld_ro<F, VPL>(vt->x + me * VPL);
       LaneV<F, VPL> prev;
       if (!first) {
-        prev = ld_stream<F, VPL>(my->y + me * VPL);
+        prev = ld_stream<F, VPL>(vt->y + me * VPL);
       } else {
 #pragma unroll
         for (int q = 0; q < VPL; ++q) { prev.re[q] = 0; prev.im[q] = 0; }
@@ -194,39 +229,35 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
 #pragma unroll
       for (int q = 0; q < VPL; ++q) { acc.re[q] = 0; acc.im[q] = 0; }
       if (!dot_only && CLS) {
-        HVal<F, CPLX_H>::load(my->diag, r).template fma<VPL>(xs, acc);
-        // the row's class (loaded one warp iteration ahead), its entry count
-        // and table row; the lane's pointers are re-read from the warp's shared
-        // slot at each use (as the ELL path does) to keep registers down
-        const int32_t tb = (int32_t)cr * my->cw;
-        const int32_t cnt = __ldg(my->soff + cr);
-        for (int k = 0; k < cnt; k += 4) {
-          const int32_t* co = my->ecol + tb + k;           // once per group of 4, as the ELL path
-          const F* cv = my->eval;
-          const CT* xp = my->x;
+        HVal<F, CPLX_H>::load(vt->diag, r).template fma<VPL>(xs, acc);
+        const int32_t kc = s_cnt[cr];
+        const int32_t tb = (int32_t)cr * vt->w;
+        const int32_t n = vt->n;
+        for (int k = 0; k < kc; k += 4) {
+          const CT* xp = vt->x;
           HVal<F, CPLX_H> h[4];
           LaneV<F, VPL> xv[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
-            const bool v = k + u < cnt;
+            const bool v = k + u < kc;
             // rows are verified equal to their class: r + offset is the row's
             // column; the clamp only keeps a bad table inside the block
-            const int32_t c = v ? min(max(r + __ldg(co + u), 0), n - 1) : r;
-            h[u] = v ? HVal<F, CPLX_H>::load(cv, tb + k + u) : HVal<F, CPLX_H>::zero();
+            const int32_t c = v ? min(max(r + s_off[tb + k + u], 0), n - 1) : r;
+            h[u] = v ? HVal<F, CPLX_H>::load_smem(s_val, tb + k + u) : HVal<F, CPLX_H>::zero();
             xv[u] = v ? ld_ro<F, VPL>(xp + ((int64_t)c * LPR + sub) * VPL) : xs;
           }
 #pragma unroll
           for (int u = 0; u < 4; ++u) h[u].template fma<VPL>(xv[u], acc);
         }
       } else if (!dot_only) {
-        HVal<F, CPLX_H>::load(my->diag, r).template fma<VPL>(xs, acc);
+        HVal<F, CPLX_H>::load(vt->diag, r).template fma<VPL>(xs, acc);
         const int32_t sidx = r >> 5, l = r & 31;
-        const int32_t* so = my->soff;
+        const int32_t* so = vt->soff;
         const int32_t off = so[sidx];
         const int32_t w = (so[sidx + 1] - off) >> 5;
         for (int k = 0; k < w; k += 4) {
-          const int32_t* cp = my->ecol + off + l;
-          const F* ev = my->eval;
+          const int32_t* cp = vt->ecol + off + l;
+          const F* ev = vt->eval;
           int32_t c[4];
           HVal<F, CPLX_H> h[4];
 #pragma unroll
@@ -235,7 +266,7 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
             c[u] = v ? __ldg(cp + (k + u) * 32) : r;
             h[u] = v ? HVal<F, CPLX_H>::load(ev, off + l + (int64_t)(k + u) * 32) : HVal<F, CPLX_H>::zero();
           }
-          const CT* xp = my->x;
+          const CT* xp = vt->x;
           LaneV<F, VPL> xv[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) xv[u] = ld_ro<F, VPL>(xp + ((int64_t)c[u] * LPR + sub) * VPL);
@@ -256,10 +287,11 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
         if (first) m1 += xs.re[q] * out.re[q] + xs.im[q] * out.im[q];
         else m1 += xs.re[q] * prev.re[q] + xs.im[q] * prev.im[q];
       }
-      if (!dot_only) st_v<F, VPL>(my->y + me * VPL, out);
+      if (!dot_only) st_v<F, VPL>(vt->y + me * VPL, out);
     }
     __syncwarp();
-    // slab partial in FP64: a fixed shuffle tree, lane 0 writes
+    // slab partial in FP64: a fixed shuffle tree, lane 0 writes (an empty
+    // slab of a lane's last tile writes zeros)
     double d0 = (double)m0, d1 = (double)m1;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -267,9 +299,9 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? 5 : 4) srv_step_
       d1 += __shfl_xor_sync(0xffffffffu, d1, o);
     }
     if (lane == 0) {
-      double* p = part + ((int64_t)j * slab_cap + begin + i) * 2;
-      p[0] = d0;
-      p[1] = d1;
+      double* pp = part + ((int64_t)j * slab_cap + (int64_t)ti * kSrvWarps + warp) * 2;
+      pp[0] = d0;
+      pp[1] = d1;
     }
   }
 }
@@ -351,13 +383,13 @@ __global__ void srv_synth_ell_kernel(int32_t n, int32_t n_slices, int32_t* soff,
 struct LaunchArgs {
   const SHdr* hdr;
   const SLane* lanes;
-  const SSlab* slabs;
+  const STile* tiles;
   double* part;
   int32_t code, j, reverse, pf, slab_cap, grid;
 };
 template <typename F, int R, bool C, bool K>
 int srv_launch(const LaunchArgs& a, cudaStream_t st) {
-  srv_step_kernel<F, R, C, K><<<a.grid, kSrvThreads, 0, st>>>(a.hdr, a.lanes, a.slabs, a.code, a.j, a.reverse, a.pf,
+  srv_step_kernel<F, R, C, K><<<a.grid, kSrvThreads, 0, st>>>(a.hdr, a.lanes, a.tiles, a.code, a.j, a.reverse, a.pf,
                                                              a.part, a.slab_cap);
   TBK_CHECK_LAUNCH();
   return TBK_OK;
@@ -367,6 +399,11 @@ int srv_occ() {
   int nb = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, srv_step_kernel<F, R, C, K>, kSrvThreads, 0);
   return nb > 0 ? nb : 1;
+}
+// tiles of a lane of n rows (slab_rows rows per slab)
+inline int32_t srv_lane_tiles(int32_t n, int32_t slab_rows) {
+  const int64_t tr = (int64_t)slab_rows * kSrvWarps;
+  return (int32_t)(((int64_t)n + tr - 1) / tr);
 }
 using LaunchFn = int (*)(const LaunchArgs&, cudaStream_t);
 using OccFn = int (*)();
@@ -601,9 +638,9 @@ struct tbk_server_s {
   int dev = 0;
   int sms = 152;
   int S = 16;
-  // class form for requests whose H~ has row classes (TBK_SERVE_CLASSES=1 at
-  // create): measured no faster than the ELL form in this kernel, so opt-in
-  bool classes = false;
+  // class form for requests whose H~ has row classes (the default;
+  // TBK_SERVE_CLASSES=0 at create keeps every request in the ELL form)
+  bool classes = true;
   double budget = 120e9, step_budget = 2e9;
   int max_resident = 4096;
   cudaStream_t st_loop = nullptr, st_admit = nullptr;
@@ -612,8 +649,8 @@ struct tbk_server_s {
   cudaMemPool_t pool = nullptr;
   AsyncAllocCtx actx;
   // round tables: one device copy, two pinned host staging copies
-  int32_t cap_lanes = 0, cap_slabs = 0, cap_reqs = 0;
-  size_t off_lanes = 0, off_slabs = 0, off_reqs = 0, tab_bytes = 0;
+  int32_t cap_lanes = 0, cap_tiles = 0, cap_reqs = 0;
+  size_t off_lanes = 0, off_tiles = 0, off_reqs = 0, tab_bytes = 0;
   DevBuf dtab, part;
   char* stage[2] = {nullptr, nullptr};
   cudaEvent_t copy_ev[2] = {nullptr, nullptr};
@@ -848,15 +885,15 @@ void admit_main(tbk_server_s* S) {
 }
 
 // ------------------------------------------------------------------ rounds
-int ensure_tables(tbk_server_s* S, int32_t lanes, int32_t slabs, int32_t reqs) {
-  if (lanes <= S->cap_lanes && slabs <= S->cap_slabs && reqs <= S->cap_reqs && S->dtab.p) return TBK_OK;
+int ensure_tables(tbk_server_s* S, int32_t lanes, int32_t tiles, int32_t reqs) {
+  if (lanes <= S->cap_lanes && tiles <= S->cap_tiles && reqs <= S->cap_reqs && S->dtab.p) return TBK_OK;
   const int32_t cl = std::max(lanes, std::max(64, S->cap_lanes * 2));
-  const int32_t cs = std::max(slabs, std::max(4096, S->cap_slabs * 2));
+  const int32_t cs = std::max(tiles, std::max(1024, S->cap_tiles * 2));
   const int32_t cr = std::max(reqs, std::max(64, S->cap_reqs * 2));
   auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
   S->off_lanes = up(sizeof(SHdr));
-  S->off_slabs = S->off_lanes + up(sizeof(SLane) * cl);
-  S->off_reqs = S->off_slabs + up(sizeof(SSlab) * cs);
+  S->off_tiles = S->off_lanes + up(sizeof(SLane) * cl);
+  S->off_reqs = S->off_tiles + up(sizeof(STile) * cs);
   S->tab_bytes = S->off_reqs + up(sizeof(SReq) * cr);
   // graphs hold the old addresses
   for (auto& kv : S->graphs) cudaGraphExecDestroy(kv.second);
@@ -868,9 +905,9 @@ int ensure_tables(tbk_server_s* S, int32_t lanes, int32_t slabs, int32_t reqs) {
     TBK_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&S->stage[b]), S->tab_bytes, cudaHostAllocDefault));
   }
   TBK_TRY(S->dtab.alloc(S->tab_bytes));
-  TBK_TRY(S->part.alloc(sizeof(double) * 2 * (size_t)cs * S->S));
+  TBK_TRY(S->part.alloc(sizeof(double) * 2 * (size_t)cs * kSrvWarps * S->S));   // one partial pair per slab
   S->cap_lanes = cl;
-  S->cap_slabs = cs;
+  S->cap_tiles = cs;
   S->cap_reqs = cr;
   return TBK_OK;
 }
@@ -885,9 +922,9 @@ int capture_graph(tbk_server_s* S, GroupMask mask, int steps, cudaGraphExec_t* o
   LaunchArgs a;
   a.hdr = reinterpret_cast<const SHdr*>(base);
   a.lanes = reinterpret_cast<const SLane*>(base + S->off_lanes);
-  a.slabs = reinterpret_cast<const SSlab*>(base + S->off_slabs);
+  a.tiles = reinterpret_cast<const STile*>(base + S->off_tiles);
   a.part = S->part.as<double>();
-  a.slab_cap = S->cap_slabs;
+  a.slab_cap = S->cap_tiles * kSrvWarps;
   TBK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   int rc = TBK_OK;
   cudaError_t e = cudaEventRecord(S->ev_fork, st);
@@ -968,23 +1005,22 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
   int32_t RS = 1;
   while (RS < left && RS < S->S) RS <<= 1;
   RS = std::min(RS, S->S);
-  int32_t n_lanes = 0, n_slabs = 0;
+  int32_t n_lanes = 0, n_tiles = 0;
   for (SrvRequest* r : order) {
-    const int32_t sr = r->slab_rows;
     n_lanes += r->n_lanes;
-    n_slabs += r->n_lanes * ((r->n + sr - 1) / sr);
+    n_tiles += r->n_lanes * srv_lane_tiles(r->n, r->slab_rows);
   }
   const int32_t n_reqs = (int32_t)order.size();
-  if (n_lanes > S->cap_lanes || n_slabs > S->cap_slabs || n_reqs > S->cap_reqs || !S->dtab.p) {
+  if (n_lanes > S->cap_lanes || n_tiles > S->cap_tiles || n_reqs > S->cap_reqs || !S->dtab.p) {
     while (!inflight.empty()) { TBK_TRY(reap(S, inflight.front())); inflight.pop_front(); }
-    TBK_TRY(ensure_tables(S, n_lanes, n_slabs, n_reqs));
+    TBK_TRY(ensure_tables(S, n_lanes, n_tiles, n_reqs));
   }
   const int b = (int)(round_id & 1);
   if (S->copy_pending[b]) { TBK_CUDA(cudaEventSynchronize(S->copy_ev[b])); S->copy_pending[b] = false; }
   char* hb = S->stage[b];
   SHdr* hdr = reinterpret_cast<SHdr*>(hb);
   SLane* lanes = reinterpret_cast<SLane*>(hb + S->off_lanes);
-  SSlab* slabs = reinterpret_cast<SSlab*>(hb + S->off_slabs);
+  STile* tiles = reinterpret_cast<STile*>(hb + S->off_tiles);
   SReq* reqs = reinterpret_cast<SReq*>(hb + S->off_reqs);
   memset(hdr, 0, sizeof(SHdr));
   Round rd;
@@ -1015,12 +1051,14 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
         L.eval = pq == TBK_PREC_MIXED ? E.cls_v32.p : pq == TBK_PREC_DD ? E.cls_vdd.p : E.cls_v64.p;
         L.cls = E.cls.as<uint8_t>();
         L.cls_w = E.cls_w;
+        L.n_cls = E.n_cls;
       } else {
         L.soff = E.slice_off.as<int32_t>();
         L.ecol = E.col.as<int32_t>();
         L.eval = pq == TBK_PREC_MIXED ? E.val32.p : pq == TBK_PREC_DD ? E.valdd.p : E.val64.p;
         L.cls = nullptr;
         L.cls_w = 0;
+        L.n_cls = 0;
       }
       L.diag = pq == TBK_PREC_MIXED ? E.diag32.p : pq == TBK_PREC_DD ? E.diagdd.p : E.diag64.p;
       L.va = r->vec[2 * c].p;
@@ -1029,11 +1067,12 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
       L.n_steps = r->n_steps;
       L.s0 = r->s0;
       L.req = qi;
-      L.slab_begin = si;
-      L.n_slabs = (r->n + sr - 1) / sr;
+      const int32_t nt = srv_lane_tiles(r->n, sr);
+      L.slab_begin = si * kSrvWarps;
+      L.n_slabs = nt * kSrvWarps;
       L.slab_rows = sr;
-      for (int32_t k = 0; k < L.n_slabs; ++k) slabs[si + k] = SSlab{li, k * sr};
-      si += L.n_slabs;
+      for (int32_t k = 0; k < nt; ++k) tiles[si + k] = STile{li, k * sr * kSrvWarps};
+      si += nt;
       ++li;
     }
     hdr->grp_count[code] = si - hdr->grp_begin[code];
@@ -1047,7 +1086,7 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
     if (q.finishing) rd.finishing.push_back(r);
   }
   hdr->n_lanes = li;
-  hdr->n_slabs = si;
+  hdr->n_tiles = si;
   hdr->n_reqs = n_reqs;
   cudaGraphExec_t gx = nullptr;
   TBK_TRY(capture_graph(S, mask, RS, &gx));
@@ -1055,7 +1094,7 @@ int launch_round(tbk_server_s* S, std::vector<SrvRequest*>& run, std::deque<Roun
   char* db = S->dtab.as<char>();
   TBK_CUDA(cudaMemcpyAsync(db, hb, sizeof(SHdr), cudaMemcpyHostToDevice, st));
   TBK_CUDA(cudaMemcpyAsync(db + S->off_lanes, lanes, sizeof(SLane) * li, cudaMemcpyHostToDevice, st));
-  TBK_CUDA(cudaMemcpyAsync(db + S->off_slabs, slabs, sizeof(SSlab) * si, cudaMemcpyHostToDevice, st));
+  TBK_CUDA(cudaMemcpyAsync(db + S->off_tiles, tiles, sizeof(STile) * si, cudaMemcpyHostToDevice, st));
   TBK_CUDA(cudaMemcpyAsync(db + S->off_reqs, reqs, sizeof(SReq) * n_reqs, cudaMemcpyHostToDevice, st));
   TBK_CUDA(cudaEventRecord(S->copy_ev[b], st));
   S->copy_pending[b] = true;
@@ -1159,14 +1198,15 @@ int autotune(tbk_server_s* S) {
       if (const char* ev = getenv("TBK_SERVE_TUNE_MB")) tune_mb = std::max(1, atoi(ev));   // tuning override
       int32_t n = (int32_t)((tune_mb << 20) / ((int64_t)rc * cs));
       const int sr = srv_slab_rows(cs, rc, n);
-      n = std::max(sr, n / sr * sr);
-      const int32_t ns = n / 32, n_slab = n / sr;
+      const int32_t tr = sr * kSrvWarps;                      // rows per tile
+      n = std::max(tr, n / tr * tr);
+      const int32_t ns = n / 32, n_tile = n / tr;
       DevBuf soff, ecol, eval, diag, va, vb, tab, prt, ccnt, coff, cval, cls;
       const size_t fs = prec == TBK_PREC_MIXED ? 4 : 8;
       if ((rc_all = soff.alloc(4 * (size_t)(ns + 1))) || (rc_all = ecol.alloc(4 * 128 * (size_t)ns)) ||
           (rc_all = eval.alloc(fs * 128 * (size_t)ns)) || (rc_all = diag.alloc(fs * 32 * (size_t)ns)) ||
           (rc_all = va.alloc((size_t)n * rc * cs)) || (rc_all = vb.alloc((size_t)n * rc * cs)) ||
-          (rc_all = prt.alloc(sizeof(double) * 2 * (size_t)n_slab)) || (rc_all = ccnt.alloc(sizeof(int32_t))) ||
+          (rc_all = prt.alloc(sizeof(double) * 2 * (size_t)n_tile * kSrvWarps)) || (rc_all = ccnt.alloc(sizeof(int32_t))) ||
           (rc_all = coff.alloc(4 * sizeof(int32_t))) || (rc_all = cval.alloc(4 * fs)) ||
           (rc_all = cls.alloc((size_t)n)))
         break;
@@ -1196,24 +1236,25 @@ int autotune(tbk_server_s* S) {
       TBK_CUDA(cudaMemsetAsync(vb.p, 0, vb.bytes, st));
       TBK_TRY(random_block_any(prec, n, rc, 0, rc, 7, va.p, st));
       const size_t off_l = (sizeof(SHdr) + 255) & ~(size_t)255, off_s = off_l + ((sizeof(SLane) + 255) & ~(size_t)255);
-      TBK_TRY(tab.alloc(off_s + sizeof(SSlab) * (size_t)n_slab));
+      TBK_TRY(tab.alloc(off_s + sizeof(STile) * (size_t)n_tile));
       for (int form = 0; form < 2; ++form) {
         const bool cf = form == 1;
         const int code = group_code(prec, rc, false, cf);
         const GroupFns fn = group_fns(code);
-        // table: one lane at step 1 of a long recursion, all its slabs in group `code`
-        std::vector<char> h(off_s + sizeof(SSlab) * (size_t)n_slab, 0);
+        // table: one lane at step 1 of a long recursion, all its tiles in group `code`
+        std::vector<char> h(off_s + sizeof(STile) * (size_t)n_tile, 0);
         SHdr* hd = reinterpret_cast<SHdr*>(h.data());
         hd->grp_begin[code] = 0;
-        hd->grp_count[code] = n_slab;
+        hd->grp_count[code] = n_tile;
         hd->n_lanes = 1;
-        hd->n_slabs = n_slab;
+        hd->n_tiles = n_tile;
         SLane* L = reinterpret_cast<SLane*>(h.data() + off_l);
         L->soff = cf ? ccnt.as<int32_t>() : soff.as<int32_t>();
         L->ecol = cf ? coff.as<int32_t>() : ecol.as<int32_t>();
         L->eval = cf ? cval.p : eval.p;
         L->cls = cf ? cls.as<uint8_t>() : nullptr;
         L->cls_w = cf ? 4 : 0;
+        L->n_cls = cf ? 1 : 0;
         L->diag = diag.p;
         L->va = va.p;
         L->vb = vb.p;
@@ -1221,18 +1262,18 @@ int autotune(tbk_server_s* S) {
         L->n_steps = 1 << 30;
         L->s0 = 1;
         L->slab_begin = 0;
-        L->n_slabs = n_slab;
+        L->n_slabs = n_tile * kSrvWarps;
         L->slab_rows = sr;
-        SSlab* sl = reinterpret_cast<SSlab*>(h.data() + off_s);
-        for (int32_t k = 0; k < n_slab; ++k) sl[k] = SSlab{0, k * sr};
+        STile* tl = reinterpret_cast<STile*>(h.data() + off_s);
+        for (int32_t k = 0; k < n_tile; ++k) tl[k] = STile{0, k * tr};
         TBK_CUDA(cudaMemcpyAsync(tab.p, h.data(), h.size(), cudaMemcpyHostToDevice, st));
         TBK_CUDA(cudaStreamSynchronize(st));
         LaunchArgs a;
         a.hdr = tab.as<SHdr>();
         a.lanes = reinterpret_cast<const SLane*>(tab.as<char>() + off_l);
-        a.slabs = reinterpret_cast<const SSlab*>(tab.as<char>() + off_s);
+        a.tiles = reinterpret_cast<const STile*>(tab.as<char>() + off_s);
         a.part = prt.as<double>();
-        a.slab_cap = n_slab;
+        a.slab_cap = n_tile * kSrvWarps;
         a.code = code;
         a.j = 0;
         const int occ = fn.occ();
