@@ -504,7 +504,8 @@ int tbk_request_footprint(const tbk_request* req, int64_t* build_peak_bytes,
  * admission charged enough). */
 int tbk_server_stats(tbk_server server, double* out, int32_t n);
 /* Launch shape chosen per group, rows[6*i ..] = {precision, width, form (0:
- * ELL, 1: row classes), grid, prefetch distance, ms per step}; returns the
+ * ELL, 1: row classes), grid, L2 prefetch mode (0: none, 1: each tile's own
+ * v_s rows at its start, 2: the next wave's tile), ms per step}; returns the
  * number of rows written. */
 int tbk_server_tuning(tbk_server server, int32_t max_rows, double* rows);
 

@@ -182,8 +182,11 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? (CLS ? 6 : 5) : 
       cur = tl.lane;
     }
     if (pf_dist > 0 && threadIdx.x == 0) {
-      // the tile this CTA reaches pf_dist iterations later: v_s, v_{s-1} rows into L2
-      const int32_t tf = t + pf_dist * (int32_t)gridDim.x;
+      // rows into L2 in bulk: pf_dist 1, this tile's v_s (its warps' later
+      // iterations and gathers find it there; v_{s-1} as well measured slower
+      // on large requests, 120 MB per wave in flight); 2, v_s and v_{s-1} of
+      // the tile this CTA takes one wave later
+      const int32_t tf = pf_dist == 2 ? t + (int32_t)gridDim.x : t;
       if (tf < cnt) {
         const STile sf = tiles[begin + (reverse ? cnt - 1 - tf : tf)];
         const SLane* Lf = lanes + sf.lane;
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? (CLS ? 6 : 5) : 
             const CT* xf = static_cast<const CT*>((sfs & 1) ? Lf->vb : Lf->va);
             const CT* pf = static_cast<const CT*>((sfs & 1) ? Lf->va : Lf->vb);
             bulk_prefetch_l2(xf + (int64_t)sf.row0 * R, nb);
-            if (sfs > 0) bulk_prefetch_l2(pf + (int64_t)sf.row0 * R, nb);
+            if (sfs > 0 && pf_dist == 2) bulk_prefetch_l2(pf + (int64_t)sf.row0 * R, nb);
           }
         }
       }
@@ -1179,9 +1182,10 @@ void loop_main(tbk_server_s* S) {
 
 // Times each candidate launch shape of every real group on a synthetic width-4
 // operator of ~256 MB per vector block — two blocks exceed the 129 MB L2, as
-// the requests that dominate the traffic do, so that the L2 prefetch distance
+// the requests that dominate the traffic do, so that the L2 prefetch mode
 // is chosen on DRAM streams (TBK_SERVE_TUNE_MB overrides) — and keeps
-// the fastest (grid, prefetch distance).  Each width is tuned twice: through
+// the fastest (grid, prefetch mode: none, the tile's own v_s rows, or the
+// next wave's tile).  Each width is tuned twice: through
 // the synthetic ELL, and in the class form with the same couplings as one
 // class (offsets +-1, +-257, clamped at the ends of the block); the complex-H
 // group of the same width and form takes the same shape.
