@@ -889,7 +889,10 @@ int ensure_classes(tbk_sparse_s* A, cudaStream_t st) {
       rof.push_back(hr[q]);
     }
   const int32_t C = (int32_t)rof.size();
-  if (C < 1 || C > kMaxClasses || (int64_t)C * std::max(W, 1) > kMaxClassEntries) return TBK_OK;
+  // entries per class rounded up to whole groups of 4 (zero tail entries: the
+  // step kernels gather a class's entries four at a time without predicates)
+  const int32_t Wt = (std::max(W, 1) + 3) / 4 * 4;
+  if (C < 1 || C > kMaxClasses || (int64_t)C * Wt > kMaxClassEntries) return TBK_OK;
   TBK_TRY(slot_id.alloc(sizeof(int32_t) * cap));
   TBK_TRY(rep_of.alloc(sizeof(int32_t) * C));
   TBK_TRY(cls.alloc((size_t)E.n_slices * 32));
@@ -902,7 +905,6 @@ int ensure_classes(tbk_sparse_s* A, cudaStream_t st) {
   class_verify_kernel<<<g, T, 0, st>>>(n, soff, ecol, v64, E.cplx, cls.as<uint8_t>(), rep_of.as<int32_t>(),
                                        flags.as<int>() + 1);
   TBK_CHECK_LAUNCH();
-  const int32_t Wt = std::max(W, 1);
   const size_t vs = E.cplx ? 2 : 1;
   DevBuf cnt, off, t64, t32, tdd;
   TBK_TRY(cnt.alloc(sizeof(int32_t) * C));

@@ -156,12 +156,18 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
       HVal<F, CPLX_H>::load(diag, r).template fma<VPL>(xs, acc);
       const int32_t cnt = s_cnt[c_cur];
       const int32_t tb = (int32_t)c_cur * ct.w;
+      // a class's tail entries up to the table width (a multiple of 4) are
+      // (offset 0, value 0): 0 x (own row), exactly what a predicated-off entry
+      // adds.  FP32 vectors take whole groups without predicates (fewer
+      // instructions and registers); the wider types keep the predicates,
+      // whose unconditional form holds more gathers in registers
+      constexpr bool WHOLE = sizeof(F) == 4;
       for (int k = 0; k < cnt; k += 4) {
         HVal<F, CPLX_H> h[4];
         LaneV<F, VPL> xv[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          const bool v = k + u < cnt;
+          const bool v = WHOLE || k + u < cnt;
           // rows are verified equal to their class, so r + offset is the
           // row's column; the clamp only keeps a bad table inside the block
           const int32_t c = v ? min(max(r + s_off[tb + k + u], 0), n - 1) : r;

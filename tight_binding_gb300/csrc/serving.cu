@@ -236,13 +236,16 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? (CLS ? 6 : 5) : 
         const int32_t kc = s_cnt[cr];
         const int32_t tb = (int32_t)cr * vt->w;
         const int32_t n = vt->n;
+        // zero tail entries up to the table width (a multiple of 4): FP32
+        // vectors take whole groups without predicates, as the moments kernel
+        constexpr bool WHOLE = sizeof(F) == 4;
         for (int k = 0; k < kc; k += 4) {
           const CT* xp = vt->x;
           HVal<F, CPLX_H> h[4];
           LaneV<F, VPL> xv[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
-            const bool v = k + u < kc;
+            const bool v = WHOLE || k + u < kc;
             // rows are verified equal to their class: r + offset is the row's
             // column; the clamp only keeps a bad table inside the block
             const int32_t c = v ? min(max(r + s_off[tb + k + u], 0), n - 1) : r;

@@ -107,7 +107,7 @@ struct EllDev {
   // row is compared entry by entry with its class's representative row.
   int32_t cls_state = 0;   // 0 not examined, 1 classes ready, -1 not applicable
   int32_t n_cls = 0;       // number of classes
-  int32_t cls_w = 0;       // table row length (max entries of a class; = max_width)
+  int32_t cls_w = 0;       // table row length: the ELL width rounded up to a multiple of 4 (zero tail)
   DevBuf cls;              // uint8 [n_slices * 32]: class of each row (0 for the tail)
   DevBuf cls_cnt;          // int32 [n_cls]: entries of each class
   DevBuf cls_off;          // int32 [n_cls * cls_w]: column - row, ELL order
