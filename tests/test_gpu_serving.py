@@ -37,6 +37,7 @@ CASES = [  # kind, L, W, M, R, precision
     ("honeycomb", 20, 1.2, 256, 64, "mixed"),
     ("kagome", 14, 0.7, 120, 8, "dd"),
     ("fcc", 6, 1.0, 64, 33, "dd"),
+    ("square", 40, 0.8, 96, 80, "mixed"),        # two complex64 lanes (64 + 16 vectors), two width groups
 ]
 
 
