@@ -157,6 +157,52 @@ def cpu_sample(cp, ri, v, n, steps, threads, R=R_VEC):
     return n * R * steps / dt, dt
 
 
+def kubo_cpu_baseline(Ht, op, M, R, steps):
+    """The reference's CPU Kubo path (TB/snippets.h:225-304 Greenwood, 306-456
+    Bastin), timed on bounded samples of the same workload and extrapolated to
+    one solve: per side M Chebyshev blocks of R vectors (Eigen's serial sparse
+    x dense product: the oracle's C walk, 1 thread), one velocity product per
+    block on the side that has an output operator plus one on an input side
+    (TB/snippets.h:337-342), then mu_nm = L^H R over K = N R (Eigen's GEMM:
+    here numpy's complex128 GEMM on all host threads, its rate measured on a
+    256 x 65,536 x 256 product)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as orc
+
+    cp, ri, v = Ht.to_csc()
+    n = len(cp) - 1
+    kets = orc.random_phase_kets(n, R, 0)
+    t0 = time.perf_counter()
+    orc.cheb_blocks(n, cp, ri, v, steps + 1, kets)              # block 0 is the input: `steps` products
+    t_step = (time.perf_counter() - t0) / steps
+    ocp, ori, ov = op.to_csc()
+    X = np.asfortranarray(kets)
+    Y = np.zeros_like(X)
+    t0 = time.perf_counter()
+    orc.lib().tbo_csc_mult(n, orc._p(ocp), orc._p(ori), orc._p(np.ascontiguousarray(ov)), int(np.iscomplexobj(ov)),
+                           R, orc._p(X), orc._p(Y))
+    t_op = time.perf_counter() - t0
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((256, 65536)) + 1j * rng.standard_normal((256, 65536))
+    B = rng.standard_normal((256, 65536)) + 1j * rng.standard_normal((256, 65536))
+    dt = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        A.conj() @ B.T
+        dt.append(time.perf_counter() - t0)
+    rate = 256 * 256 * 65536 / min(dt)                             # complex multiply-adds per second
+    K = n * R
+    recursion_s = 2 * M * t_step + (M + 1) * t_op
+    gemm_s = M * M * K / rate
+    return {"kind": "port", "value_s": recursion_s + gemm_s, "unit": "s per solve (extrapolated)",
+            "recursion_s": recursion_s, "gemm_s": gemm_s,
+            "recursion": {"cores": 1, "s_per_step": t_step, "steps_timed": steps, "operator_product_s": t_op},
+            "gemm": {"cores": os.cpu_count(), "complex_macs_per_s": rate, "macs": M * M * K},
+            "sample": "%d recursion steps and one velocity product of the workload's H~ (%d sites, R=%d), and a "
+                      "256 x 65,536 x 256 complex128 GEMM; 2 M steps + (M + 1) products + M^2 N R MACs" %
+                      (steps, n, R)}
+
+
 def reference_gpu_algorithm(N, cp, ri, v, kets_ptr, R, n_mom):
     """The reference's own GPU algorithm (tight_binding/numerics_cuda.cu:190-255,
     restated in baseline/cusparse_kpm.cu): per call the CSC and the split Re / Im
@@ -498,12 +544,14 @@ def peaks_tensor():
 
 
 def run_kubo(config: int, tensor: bool = True, recursion: str = "mixed", fuse_ops: bool = False, moments: int = 0,
-             budget_gb: float = 0.0, parity: bool = False):
+             budget_gb: float = 0.0, parity: bool = False, cpu: bool = True):
     """Kubo legs: config 3 (Bastin sigma_xy, square 256^2 open-x / periodic-y, Landau
     flux 1/64, M = 512, R = 16, seed 2) or config 5 (Greenwood sigma_xx, FCC 128^3
     periodic, on-site U[-1,1] seed 4, M = 1024, R = 8).  parity (config 3): also
     the FP64 reference form (complex128 recursion and blocks, FP64 GEMM) on the
-    same seeded vectors, and max |d sigma_xy| / max |sigma_xy| against it."""
+    same seeded vectors, and max |d sigma_xy| / max |sigma_xy| against it.
+    cpu: the reference's CPU path on bounded samples, extrapolated
+    (kubo_cpu_baseline)."""
     import tight_binding_gb300 as tb
 
     sig = {}
@@ -522,6 +570,7 @@ def run_kubo(config: int, tensor: bool = True, recursion: str = "mixed", fuse_op
             result = {"E_F_points": int(len(out["E"])), "sigma_xy_at_E0": float(out["sigma_re"][len(out["E"]) // 2])}
             sig["args"] = (H, X.op_position(0), X.op_position(1), M, -4.0, 4.0)
             sig["R"] = R
+            sig["cpu"] = (H, X.op_position(1), M, R, -4.0, 4.0, 16)        # input side: v_y r
             sig["sigma"] = out["sigma_re"]
             workload = "Kubo-Bastin sigma_xy: square 256x256 open-x/periodic-y, Landau flux 1/64, M=512, R=16 seed 2"
         else:
@@ -533,6 +582,7 @@ def run_kubo(config: int, tensor: bool = True, recursion: str = "mixed", fuse_op
                                                       E_min=-13.0, E_max=13.0, tensor=tensor, recursion=recursion,
                                                       fuse_ops=fuse_ops, budget_gb=budget_gb)
             result = {"energies": int(len(eps)), "sigma_xx_max": float(np.max(sigma))}
+            sig["cpu"] = (H, X.op_position(0), M, R, -13.0, 13.0, 2)
             workload = "Kubo-Greenwood sigma_xx: FCC 128^3 periodic, disorder U[-1,1] seed 4, M=1024, R=8"
         return time.perf_counter() - t0, workload, result
 
@@ -558,6 +608,12 @@ def run_kubo(config: int, tensor: bool = True, recursion: str = "mixed", fuse_op
                                "bytes": "algorithmic: work vectors + matrix per pass + complex64 stores"}
     if tensor:
         line["tensor_util"] = line["gemm_tflops_issued"] / peak
+    if cpu:
+        H, pos, M_c, R_c, lo, hi, steps = sig["cpu"]
+        Ht = tb.GreenFunction(M_c, H, lo, hi).scaled_HE
+        cb = kubo_cpu_baseline(Ht, tb.commutator(Ht, pos), M_c, R_c, steps)
+        cb["speedup_vs_wall"] = cb["value_s"] / wall
+        line["cpu_baseline"] = cb
     if parity and config == 3:
         t0 = time.perf_counter()
         ref = tb.conductivity_Kubo_Bastin(*sig["args"], R=sig["R"], seed=2, recursion="fp64", fp64_blocks=True)
