@@ -279,6 +279,54 @@ struct HVal<F, true> {
   }
 };
 
+// out = 2 acc - prev for the lane's elements.  Double-float: both parts of an
+// element in packed f32x2 arithmetic; 2 acc is exact, so the scalar dd(2) *
+// acc is the pair's TwoSum (2 hi, 2 lo), and the subtraction is the scalar
+// dd addition of -prev, operation for operation: the same values.
+__device__ __forceinline__ void dd_out2(dd ar, dd ai, dd pr, dd pi, dd& outr, dd& outi) {
+  const uint64_t neg = f2_pack(-1.f, -1.f);
+  const uint64_t h = f2_add(f2_pack(ar.hi, ai.hi), f2_pack(ar.hi, ai.hi));
+  const uint64_t l = f2_add(f2_pack(ar.lo, ai.lo), f2_pack(ar.lo, ai.lo));
+  const uint64_t s = f2_add(h, l);                             // fast TwoSum (|h| >= |l|)
+  const uint64_t sl = f2_sub(l, f2_sub(s, h));
+  const uint64_t yh = f2_mul(neg, f2_pack(pr.hi, pi.hi)), yl = f2_mul(neg, f2_pack(pr.lo, pi.lo));
+  const uint64_t s2 = f2_add(s, yh);                           // the dd addition
+  const uint64_t bb = f2_sub(s2, s);
+  uint64_t e = f2_add(f2_sub(s, f2_sub(s2, bb)), f2_sub(yh, bb));
+  e = f2_add(e, f2_add(sl, yl));
+  const uint64_t o = f2_add(s2, e);
+  const uint64_t ol = f2_sub(e, f2_sub(o, s2));
+  f2_unpack(o, outr.hi, outi.hi);
+  f2_unpack(ol, outr.lo, outi.lo);
+}
+template <typename F, int VPL>
+__device__ __forceinline__ void recur_out(const LaneV<F, VPL>& acc, const LaneV<F, VPL>& prev, LaneV<F, VPL>& out) {
+#pragma unroll
+  for (int q = 0; q < VPL; ++q) {
+    if constexpr (is_dd<F>) {
+      dd_out2(acc.re[q], acc.im[q], prev.re[q], prev.im[q], out.re[q], out.im[q]);
+    } else {
+      out.re[q] = F(2) * acc.re[q] - prev.re[q];
+      out.im[q] = F(2) * acc.im[q] - prev.im[q];
+    }
+  }
+}
+// m += Re sum_q conj(a_q) b_q over the lane's elements.  Double-float: the
+// terms accumulate unnormalised in the manner of Dot2 (dd_fma_acc), which the
+// final conversion (double) hi + (double) lo takes exactly.
+template <typename F, int VPL>
+__device__ __forceinline__ void dot_acc(const LaneV<F, VPL>& a, const LaneV<F, VPL>& b, F& m) {
+#pragma unroll
+  for (int q = 0; q < VPL; ++q) {
+    if constexpr (is_dd<F>) {
+      dd_fma_acc(a.re[q], b.re[q], m);
+      dd_fma_acc(a.im[q], b.im[q], m);
+    } else {
+      m += a.re[q] * b.re[q] + a.im[q] * b.im[q];
+    }
+  }
+}
+
 // a row sum built by HVal::fma, ready for use: double-float sums are
 // normalised (no-op for float and double)
 template <typename F, int VPL>

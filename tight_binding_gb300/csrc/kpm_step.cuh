@@ -222,11 +222,8 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     finish_acc<F, VPL>(acc);
     if constexpr (KST == 2) finish_acc<F, VPL>(vacc);
     LaneV<F, VPL> out;
-#pragma unroll
-    for (int q = 0; q < VPL; ++q) {
-      if constexpr (FIRST) { out.re[q] = acc.re[q]; out.im[q] = acc.im[q]; }
-      else { out.re[q] = F(2) * acc.re[q] - prev.re[q]; out.im[q] = F(2) * acc.im[q] - prev.im[q]; }
-    }
+    if constexpr (FIRST) out = acc;
+    else recur_out<F, VPL>(acc, prev, out);
     if constexpr (KST == 3) {
       // Clenshaw step of a Chebyshev expansion: b_k = 2 H b_{k+1} - b_{k+2} + c_k v
       const LaneV<F, VPL> vv = ld_ro<F, VPL>(static_cast<const CT*>(ks.addv) + me * VPL);
@@ -242,18 +239,12 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
     if constexpr (KST != 0) {
     } else if constexpr (BRAKET) {
       const LaneV<F, VPL> b = ld_ro<F, VPL>(bras + me * VPL);
-#pragma unroll
-      for (int q = 0; q < VPL; ++q) {
-        m0 += b.re[q] * out.re[q] + b.im[q] * out.im[q];
-        if constexpr (FIRST) m1 += b.re[q] * xs.re[q] + b.im[q] * xs.im[q];
-      }
+      dot_acc<F, VPL>(b, out, m0);
+      if constexpr (FIRST) dot_acc<F, VPL>(b, xs, m1);
     } else {
-#pragma unroll
-      for (int q = 0; q < VPL; ++q) {
-        m0 += xs.re[q] * xs.re[q] + xs.im[q] * xs.im[q];
-        if constexpr (FIRST) m1 += xs.re[q] * out.re[q] + xs.im[q] * out.im[q];
-        else m1 += xs.re[q] * prev.re[q] + xs.im[q] * prev.im[q];
-      }
+      dot_acc<F, VPL>(xs, xs, m0);
+      if constexpr (FIRST) dot_acc<F, VPL>(xs, out, m1);
+      else dot_acc<F, VPL>(xs, prev, m1);
     }
     if (store) st_v<F, VPL>(y + me * VPL, out);
     if constexpr (KST == 1) {

@@ -282,17 +282,11 @@ __global__ void __launch_bounds__(kSrvThreads, sizeof(F) == 4 ? (CLS ? 6 : 5) : 
       }
       finish_acc<F, VPL>(acc);
       LaneV<F, VPL> out;
-#pragma unroll
-      for (int q = 0; q < VPL; ++q) {
-        if (first) { out.re[q] = acc.re[q]; out.im[q] = acc.im[q]; }
-        else { out.re[q] = F(2) * acc.re[q] - prev.re[q]; out.im[q] = F(2) * acc.im[q] - prev.im[q]; }
-      }
-#pragma unroll
-      for (int q = 0; q < VPL; ++q) {
-        m0 += xs.re[q] * xs.re[q] + xs.im[q] * xs.im[q];
-        if (first) m1 += xs.re[q] * out.re[q] + xs.im[q] * out.im[q];
-        else m1 += xs.re[q] * prev.re[q] + xs.im[q] * prev.im[q];
-      }
+      if (first) out = acc;
+      else recur_out<F, VPL>(acc, prev, out);
+      dot_acc<F, VPL>(xs, xs, m0);
+      if (first) dot_acc<F, VPL>(xs, out, m1);
+      else dot_acc<F, VPL>(xs, prev, m1);
       if (!dot_only) st_v<F, VPL>(vt->y + me * VPL, out);
     }
     __syncwarp();
