@@ -832,7 +832,8 @@ def run_small(args):
     vector block): reports per-solve latency p50/p99 over --steps solves of the
     resident plan (FP64, mixed and double-float, doubling; per-step launches
     replayed as a CUDA graph, without the graph, and the opt-in one-launch
-    cluster recursion), the
+    recursion: one CTA per vector where H~ has row classes and a complex64 or
+    double-float vector fits one SM, else a cluster per vector), the
     drop-in C-ABI call with host buffers (H~ uploaded every call, as the
     reference's cuSPARSE path does), and the CPU oracle on the whole solve."""
     import torch
@@ -857,9 +858,10 @@ def run_small(args):
            "solves": steps}
     ref_mu = None
     for name, prec, extra in (("fp64", "fp64", 0), ("fp64_no_graph", "fp64", capi.FLAG_NO_GRAPH),
-                              ("fp64_cluster", "fp64", capi.FLAG_PERSISTENT), ("mixed", "mixed", 0),
-                              ("mixed_cluster", "mixed", capi.FLAG_PERSISTENT),
-                              ("mixed_two_step", "mixed", capi.FLAG_TWO_STEP), ("dd", "dd", 0)):
+                              ("fp64_one_launch", "fp64", capi.FLAG_PERSISTENT), ("mixed", "mixed", 0),
+                              ("mixed_one_launch", "mixed", capi.FLAG_PERSISTENT),
+                              ("mixed_two_step", "mixed", capi.FLAG_TWO_STEP), ("dd", "dd", 0),
+                              ("dd_one_launch", "dd", capi.FLAG_PERSISTENT)):
         sol = tb.KpmSolver(Ht, R, precision=prec, doubling=True, flags=capi.FLAG_DEVICE_PTRS | extra)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * steps)]
         for _ in range(args.warmup + 2):

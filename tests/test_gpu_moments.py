@@ -252,8 +252,9 @@ def test_graph_replay_matches_direct_launches(gpu, precision, doubling):
                                                        ("mixed", True, True, 8), ("mixed", False, False, 5),
                                                        ("dd", True, False, 4), ("dd", False, True, 2)])
 def test_one_launch_recursion_matches_oracle(gpu, precision, doubling, cplx, R):
-    """TBK_FLAG_PERSISTENT: the whole recursion in one launch, one thread-block
-    cluster per random vector: moments against the oracle and against the
+    """TBK_FLAG_PERSISTENT: the whole recursion in one launch (one CTA per
+    complex64 vector where H~ has row classes, else one thread-block cluster
+    per random vector): moments against the oracle and against the
     one-launch-per-step path."""
     tb = gpu
     from tight_binding_gb300 import capi

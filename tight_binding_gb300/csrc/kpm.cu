@@ -422,6 +422,8 @@ struct tbk_kpm_s {
   } gkey, seen;
   int small_state = 0;              // one-launch recursion: 0 undecided, 1 used, -1 not applicable
   SmallLayout slay{};
+  bool cta = false;                 // the one-launch recursion is one CTA per vector (kpm_cta_kernel)
+  CtaLayout clay{};
 };
 
 // TBK_TRACE=1: every host-input solve prints its phases (upload, kets load,
@@ -582,15 +584,60 @@ static void* small_kernel(int prec, bool cplx, bool braket) {
   return cplx ? small_kernel_ptr<float, true>(braket) : small_kernel_ptr<float, false>(braket);
 }
 
-// decides once per plan whether the one-launch recursion applies and lays out
-// its shared memory: rows per CTA a power of two >= 32, at most 8 CTAs per
-// cluster, at most 2 rows per thread
+template <typename F, bool CPLX_H>
+static void* cta_kernel_ptr(bool braket) {
+  return braket ? reinterpret_cast<void*>(kpm_cta_kernel<F, CPLX_H, true>)
+                : reinterpret_cast<void*>(kpm_cta_kernel<F, CPLX_H, false>);
+}
+static void* cta_kernel(bool cplx, bool braket) {
+  return cplx ? cta_kernel_ptr<float, true>(braket) : cta_kernel_ptr<float, false>(braket);
+}
+
+// decides once per plan whether the one-launch recursion (TBK_FLAG_PERSISTENT)
+// applies and lays out its shared memory.  Complex64 vectors of a matrix with
+// row classes that fit one SM: one CTA per vector (kpm_cta_kernel; the
+// 4,096-site, 8-vector solve: 0.40 ms against 0.63 ms for the per-step
+// launches replayed as a graph).  Otherwise a cluster per vector: rows per CTA
+// a power of two >= 32, at most 8 CTAs per cluster, at most 2 rows per
+// thread.  (One CTA per double-float vector measured 0.91 ms against 0.74 ms:
+// one SM's FP32 pipe sets the pace.)  Opt-in: the one-launch forms group the
+// moment sums per vector, so their bits differ from the per-step kernels'
+// (which the class and ELL forms share).
 static int plan_small(tbk_kpm_s* P, bool tma) {
   if (P->small_state != 0) return TBK_OK;
   P->small_state = -1;
   if (!(P->flags & TBK_FLAG_PERSISTENT) || P->n_chunks != 1 || tma || (P->flags & TBK_FLAG_TWO_STEP)) return TBK_OK;
   const EllDev& E = P->H->ell;
   const int32_t n = (int32_t)P->n;
+  if (P->use_cls && P->prec == TBK_PREC_MIXED) {
+    CtaLayout C;
+    C.n = n;
+    C.n_cls = E.n_cls;
+    C.w = E.cls_w;
+    C.csz = (int32_t)P->csize;
+    C.vb = (P->prec == TBK_PREC_MIXED ? 4 : 8) * (E.cplx ? 2 : 1);
+    if ((int64_t)C.bytes() <= kSmallSmemBytes) {
+      bool ok = true;
+      for (int b = 0; b < 2 && ok; ++b)
+        if (cudaFuncSetAttribute(cta_kernel(E.cplx != 0, b == 1), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 C.bytes()) != cudaSuccess) {
+          cudaGetLastError();
+          ok = false;
+        }
+      if (ok) {
+        P->clay = C;
+        P->cta = true;
+        P->slay = SmallLayout{};
+        P->slay.cs = 1;                   // partials: one pair per vector and step
+        P->small_state = 1;
+        if (P->R > P->grid_max) {
+          P->grid_max = P->R;
+          P->cap_steps = 0;
+        }
+        return TBK_OK;
+      }
+    }
+  }
   int32_t rpc = 32, lg = 5;
   while ((int64_t)rpc * kClusterMax < n) { rpc <<= 1; ++lg; }
   if (rpc > 2 * kSmallThreadsMax) return TBK_OK;
@@ -675,8 +722,27 @@ static int launch_small_t(tbk_kpm_s* P, bool braket, int32_t n_steps, cudaStream
   return TBK_OK;
 }
 
+template <typename F, bool CPLX_H>
+static int launch_cta_t(tbk_kpm_s* P, bool braket, int32_t n_steps, cudaStream_t st) {
+  using CT = typename C2<F>::T;
+  const EllDev& E = P->H->ell;
+  const CtaLayout C = P->clay;
+  const ClassTab ct = class_tab(E, P->prec);
+  const F* dg = static_cast<const F*>(ell_diag(E, P->prec));
+  const CT* k = static_cast<const CT*>(P->va.p);
+  const CT* b = braket ? static_cast<const CT*>(P->bras.p) : nullptr;
+  double* pt = P->part.as<double>();
+  if (braket)
+    kpm_cta_kernel<F, CPLX_H, true><<<P->R, cta_threads<F>(), C.bytes(), st>>>(n_steps, P->Rc, C, ct, dg, k, b, pt);
+  else
+    kpm_cta_kernel<F, CPLX_H, false><<<P->R, cta_threads<F>(), C.bytes(), st>>>(n_steps, P->Rc, C, ct, dg, k, b, pt);
+  TBK_CHECK_LAUNCH();
+  return TBK_OK;
+}
+
 static int launch_small(tbk_kpm_s* P, bool braket, int32_t n_steps, cudaStream_t st) {
   const bool c = P->H->ell.cplx != 0;
+  if (P->cta) return c ? launch_cta_t<float, true>(P, braket, n_steps, st) : launch_cta_t<float, false>(P, braket, n_steps, st);
   if (P->prec == TBK_PREC_FP64) return c ? launch_small_t<double, true>(P, braket, n_steps, st)
                                          : launch_small_t<double, false>(P, braket, n_steps, st);
   if (P->prec == TBK_PREC_DD) return c ? launch_small_t<dd, true>(P, braket, n_steps, st)

@@ -17,7 +17,8 @@
 // Partials: part[(step * 2 + slot) * nblk + CTA], the layout the fixed-order
 // reduction of the multi-launch path reads (one chunk).
 //
-// Opt-in (TBK_FLAG_PERSISTENT).  Measured on the 4,096-site, 8-vector case
+// Opt-in (TBK_FLAG_PERSISTENT) where kpm_cta_kernel below does not apply.
+// Measured on the 4,096-site, 8-vector case
 // (M = 256): 0.84 ms FP64 and 0.57 ms complex64 per solve, against 0.71 ms and
 // 0.58 ms for the per-step kernels replayed as a CUDA graph.  The steps stall
 // on distributed-shared-memory reads and the cluster barrier (short-scoreboard
@@ -194,6 +195,159 @@ __global__ void __launch_bounds__(kSmallThreadsMax) kpm_cluster_kernel(
       }
       part[((int64_t)s * 2 + 0) * gridDim.x + blockIdx.x] = a;
       part[((int64_t)s * 2 + 1) * gridDim.x + blockIdx.x] = b;
+    }
+  }
+}
+
+// One CTA per random complex64 vector for matrices with row classes
+// (kpm_step.cuh's class form): the whole recursion of a vector in one SM's
+// shared memory — v_n and v_{n-1} of every row, the diagonal, each row's class
+// byte and the class table (84 KB for 4,096 sites) — with one CTA barrier
+// between steps and no other SM involved.  Rows are computed as the step
+// kernel's class form computes them (diagonal first, then the class's entries
+// in order, whole groups of 4 over the zero-padded table), so the vectors
+// take the same values; the moment sums are grouped per vector, in
+// double-float trees on the FP32 pipe (one SM's FP64 rate would set the step
+// time), with FP64 only for the step's result.  Templated on the vector
+// precision, used for complex64.
+struct CtaLayout {
+  int32_t n, n_cls, w, csz, vb;           // rows, classes, entries per class, vector / matrix element bytes
+  __host__ __device__ static int32_t up16(int32_t b) { return (b + 15) / 16 * 16; }
+  __host__ __device__ int32_t off_x() const { return 0; }
+  __host__ __device__ int32_t off_diag() const { return up16(2 * n * csz); }
+  __host__ __device__ int32_t off_tval() const { return up16(off_diag() + n * vb); }
+  __host__ __device__ int32_t off_toff() const { return up16(off_tval() + n_cls * w * vb); }
+  __host__ __device__ int32_t off_tcnt() const { return off_toff() + n_cls * w * 4; }
+  __host__ __device__ int32_t off_cls() const { return up16(off_tcnt() + n_cls * 4); }
+  __host__ __device__ int32_t bytes() const { return up16(off_cls() + n); }
+};
+template <typename F>
+__host__ __device__ constexpr int cta_threads() { return sizeof(F) == 4 ? 1024 : 512; }
+__device__ __forceinline__ dd dd_of(float v) { return dd(v, 0.f); }
+__device__ __forceinline__ dd dd_of(dd v) { return dd_norm(v); }   // TwoSum: an unnormalised Dot2 pair
+
+template <typename F, bool CPLX_H, bool BRAKET>
+__global__ void __launch_bounds__(cta_threads<F>()) kpm_cta_kernel(
+    int32_t n_steps, int32_t Rp, CtaLayout L, const ClassTab ct, const F* __restrict__ diag,
+    const typename C2<F>::T* __restrict__ kets, const typename C2<F>::T* __restrict__ bras,
+    double* __restrict__ part) {
+  using CT = typename C2<F>::T;
+  constexpr int VW = CPLX_H ? 2 : 1;     // F values per matrix value
+  constexpr int NT = cta_threads<F>();
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ dd wsum[2][2][NT / 32];
+  const int32_t n = L.n, vec = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  CT* xa = reinterpret_cast<CT*>(sm + L.off_x());
+  CT* xb = xa + n;
+  F* dg = reinterpret_cast<F*>(sm + L.off_diag());
+  F* tv = reinterpret_cast<F*>(sm + L.off_tval());
+  int32_t* to = reinterpret_cast<int32_t*>(sm + L.off_toff());
+  int32_t* tc = reinterpret_cast<int32_t*>(sm + L.off_tcnt());
+  uint8_t* cl = sm + L.off_cls();
+  {  // table, diagonal and class bytes as 4-byte words / bytes; the kets' column of this vector
+    const int32_t ne = L.n_cls * L.w;
+    const int32_t vw = ne * VW * (int32_t)sizeof(F) / 4, dw = n * VW * (int32_t)sizeof(F) / 4;
+    const uint32_t* gv = static_cast<const uint32_t*>(ct.val);
+    const uint32_t* gd = reinterpret_cast<const uint32_t*>(diag);
+    for (int32_t q = threadIdx.x; q < vw; q += NT) reinterpret_cast<uint32_t*>(tv)[q] = __ldg(gv + q);
+    for (int32_t q = threadIdx.x; q < ne; q += NT) to[q] = __ldg(ct.off + q);
+    for (int32_t q = threadIdx.x; q < L.n_cls; q += NT) tc[q] = __ldg(ct.cnt + q);
+    for (int32_t q = threadIdx.x; q < dw; q += NT) reinterpret_cast<uint32_t*>(dg)[q] = __ldg(gd + q);
+    for (int32_t q = threadIdx.x; q < n; q += NT) {
+      cl[q] = __ldg(ct.cls + q);
+      xa[q] = kets[(int64_t)q * Rp + vec];
+      CT z;
+      z.x = F(0);
+      z.y = F(0);
+      xb[q] = z;
+    }
+  }
+  __syncthreads();
+  for (int32_t s = 0; s < n_steps; ++s) {
+    const bool first = s == 0;
+    const bool last_dot = !BRAKET && s == n_steps - 1 && s > 0;   // dots only, no product
+    const CT* x = (s & 1) ? xb : xa;
+    CT* y = (s & 1) ? xa : xb;                  // v_{s-1} on entry, v_{s+1} on exit
+    F m0 = 0, m1 = 0;                           // this thread's rows (FP32 pipe; Dot2 for double-float)
+    for (int32_t r = threadIdx.x; r < n; r += NT) {
+      LaneV<F, 1> xs, prev, out;
+      xs.re[0] = x[r].x;
+      xs.im[0] = x[r].y;
+      prev.re[0] = y[r].x;
+      prev.im[0] = y[r].y;
+      if (!last_dot) {
+        LaneV<F, 1> acc;
+        acc.re[0] = F(0);
+        acc.im[0] = F(0);
+        HVal<F, CPLX_H>::load_smem(dg, r).template fma<1>(xs, acc);
+        const int32_t c = cl[r];
+        const int32_t cnt = tc[c], tb = c * L.w;
+        for (int32_t k = 0; k < cnt; k += 4) {
+          HVal<F, CPLX_H> h[4];
+          LaneV<F, 1> xv[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            // rows are verified equal to their class: r + offset is the row's
+            // column; the clamp only keeps a bad table inside the vector
+            const int32_t col = min(max(r + to[tb + k + u], 0), n - 1);
+            h[u] = HVal<F, CPLX_H>::load_smem(tv, tb + k + u);
+            xv[u].re[0] = x[col].x;
+            xv[u].im[0] = x[col].y;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) h[u].template fma<1>(xv[u], acc);
+        }
+        finish_acc<F, 1>(acc);
+        if (first) out = acc;
+        else recur_out<F, 1>(acc, prev, out);
+      } else {
+        out = prev;
+      }
+      if constexpr (BRAKET) {
+        const CT bv = bras[(int64_t)r * Rp + vec];
+        LaneV<F, 1> b;
+        b.re[0] = bv.x;
+        b.im[0] = bv.y;
+        dot_acc<F, 1>(b, out, m0);
+        if (first) dot_acc<F, 1>(b, xs, m1);
+      } else {
+        dot_acc<F, 1>(xs, xs, m0);
+        if (first) dot_acc<F, 1>(xs, out, m1);
+        else dot_acc<F, 1>(xs, prev, m1);
+      }
+      if (!last_dot) {
+        CT o;
+        o.x = out.re[0];
+        o.y = out.im[0];
+        y[r] = o;
+      }
+    }
+    // sums of the vector: double-float trees on the FP32 pipe (GB300's FP64
+    // rate on one SM would set the step time), FP64 only for the result
+    dd a0 = dd_of(m0), a1 = dd_of(m1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 = a0 + dd(__shfl_xor_sync(0xffffffffu, a0.hi, o), __shfl_xor_sync(0xffffffffu, a0.lo, o));
+      a1 = a1 + dd(__shfl_xor_sync(0xffffffffu, a1.hi, o), __shfl_xor_sync(0xffffffffu, a1.lo, o));
+    }
+    if (lane == 0) {
+      wsum[s & 1][0][warp] = a0;
+      wsum[s & 1][1][warp] = a1;
+    }
+    __syncthreads();                             // step done: y becomes the next x
+    if (warp == 0) {
+      dd b0 = lane < NT / 32 ? wsum[s & 1][0][lane] : dd(0.f, 0.f);
+      dd b1 = lane < NT / 32 ? wsum[s & 1][1][lane] : dd(0.f, 0.f);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        b0 = b0 + dd(__shfl_xor_sync(0xffffffffu, b0.hi, o), __shfl_xor_sync(0xffffffffu, b0.lo, o));
+        b1 = b1 + dd(__shfl_xor_sync(0xffffffffu, b1.hi, o), __shfl_xor_sync(0xffffffffu, b1.lo, o));
+      }
+      if (lane == 0) {
+        part[((int64_t)s * 2 + 0) * gridDim.x + blockIdx.x] = (double)b0;
+        part[((int64_t)s * 2 + 1) * gridDim.x + blockIdx.x] = (double)b1;
+      }
     }
   }
 }
