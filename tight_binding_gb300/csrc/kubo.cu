@@ -19,6 +19,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
 #include <cmath>
 #include <cstdlib>
 #include <mutex>
@@ -285,6 +287,64 @@ struct KuboTiming { double ms_blocks = 0, ms_gemm = 0, gemm_flops = 0, block_byt
 KuboTiming g_kubo_timing;        // the last solve's timing (calls may come from several threads)
 std::mutex g_kubo_timing_mu;
 
+// TBK_TRACE=1: tbk_kubo_mu prints the host time of its phases to stderr
+// (synchronising at each phase boundary, which it otherwise does not)
+struct PhaseTrace {
+  bool on;
+  cudaStream_t st;
+  std::chrono::steady_clock::time_point t0;
+  std::vector<std::pair<const char*, double>> marks;
+  explicit PhaseTrace(cudaStream_t s) : st(s), t0(std::chrono::steady_clock::now()) {
+    const char* e = getenv("TBK_TRACE");
+    on = e && atoi(e) != 0;
+  }
+  void mark(const char* name) {
+    if (!on) return;
+    cudaStreamSynchronize(st);
+    marks.emplace_back(name, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+  }
+  ~PhaseTrace() {
+    if (!on) return;
+    double prev = 0.0;
+    fprintf(stderr, "tbk_kubo_mu phases (ms):");
+    for (auto& m : marks) {
+      fprintf(stderr, " %s %.2f", m.first, m.second - prev);
+      prev = m.second;
+    }
+    fprintf(stderr, "\n");
+  }
+};
+
+// The stored blocks and work blocks of a call made outside a server come
+// from a stream-ordered pool that keeps up to kKuboPoolKeep bytes between
+// calls: stores of that size are then reused instead of mapped and unmapped
+// every call (config 3: 8.6 GB, whose cudaFree took 5.7 ms of a 36 ms call).
+// Larger stores keep plain allocations (a 137 GB store from the pool, then
+// trimmed, measured 0.2 s slower than cudaMalloc and cudaFree); each call
+// trims the pool back to kKuboPoolKeep before it returns.
+constexpr uint64_t kKuboPoolKeep = 16ull << 30;
+cudaMemPool_t kubo_pool() {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); return nullptr; }
+  std::lock_guard<std::mutex> lk(mu);
+  if (!pools[dev]) {
+    cudaMemPoolProps pp = {};
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = dev;
+    if (cudaMemPoolCreate(&pools[dev], &pp) != cudaSuccess) {
+      cudaGetLastError();
+      pools[dev] = nullptr;
+      return nullptr;
+    }
+    uint64_t keep = kKuboPoolKeep;
+    cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  return pools[dev];
+}
+
 int pick_chunk(int R) {
   int c = 1;
   while (c < R && c < 32) c <<= 1;
@@ -308,9 +368,14 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   for (auto* o : ops)
     if (o && (o->rows != Ht->rows || o->cols != Ht->cols)) return fail(TBK_ERR_INVALID, "tbk_kubo_mu: operator size mismatch");
   cudaStream_t st = as_stream(stream);
+  PhaseTrace trace(st);
+  // outside a server (which sets its own pool): stores and work blocks that
+  // the pool keeps come from kubo_pool (decided below, once their size is known)
+  AsyncAllocCtx kctx{};
   const int32_t n = Ht->rows;
   TBK_TRY(ensure_ell(Ht, st));
   for (auto* o : ops) if (o) TBK_TRY(ensure_ell(o, st));
+  trace.mark("ell");
   const int64_t n_pad = (int64_t)Ht->ell.n_slices * 32;
   // chunk of random vectors: both stored sides within the budget
   int Rc = pick_chunk(R);
@@ -340,8 +405,17 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   const size_t csz = prec == TBK_PREC_MIXED ? sizeof(float2) : sizeof(double2);
   DevBuf Ls, Rs, work, partd, part, macc, gdev, kstage;
   const int64_t blk16 = (blk + 15) / 16 * 16;           // K padded to whole 16-element tiles (zeros)
-  TBK_TRY(Ls.alloc((size_t)sel * blk16 * M));
-  TBK_TRY(Rs.alloc((size_t)sel * blk16 * M));
+  if (!tl_async_alloc && 2.0 * sel * blk16 * M + 12.0 * csz * blk <= (double)kKuboPoolKeep) {
+    kctx.pool = kubo_pool();
+    kctx.stream = st;
+  }
+  {
+    const AsyncAllocCtx* outer = tl_async_alloc;
+    if (kctx.pool) tl_async_alloc = &kctx;
+    const int a = Ls.alloc((size_t)sel * blk16 * M), b = a == TBK_OK ? Rs.alloc((size_t)sel * blk16 * M) : a;
+    tl_async_alloc = outer;
+    TBK_TRY(b);
+  }
   // both sides as one recursion of width 2 Rc (TBK_MU_BOTH_SIDES) when every
   // output operator can be fused into the step (the gathers move twice the
   // bytes per row; the stored values are the same bits)
@@ -353,9 +427,26 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     TBK_TRY(same_ell_structure(Ht, o, &same, st));
     both = same;
   }
-  TBK_TRY(work.alloc(csz * blk * (both ? 12 : 6)));
-  TBK_CUDA(cudaMemsetAsync(Ls.p, 0, Ls.bytes, st));
-  TBK_CUDA(cudaMemsetAsync(Rs.p, 0, Rs.bytes, st));
+  {
+    const AsyncAllocCtx* outer = tl_async_alloc;
+    if (kctx.pool) tl_async_alloc = &kctx;
+    const int a = work.alloc(csz * blk * (both ? 12 : 6));
+    tl_async_alloc = outer;
+    TBK_TRY(a);
+  }
+  {
+    // the stores write every k < n Rc of every block; the entries of padded
+    // rows (n <= row < n_pad) and of the K tail up to whole 16-element tiles
+    // must read as zero.  In the K-tiled layout, element ((k/16) M + m) 16 +
+    // k%16, they all lie in the K tiles from floor(n Rc / 16) on: one
+    // contiguous region (the stores overwrite its written part afterwards)
+    const int64_t kt0 = (int64_t)n * Rc / 16, kt1 = blk16 / 16;
+    const size_t tile = (size_t)sel * 16 * M;           // bytes of one K tile of all M blocks
+    if (kt1 > kt0) {
+      TBK_CUDA(cudaMemsetAsync(Ls.as<char>() + kt0 * tile, 0, (size_t)(kt1 - kt0) * tile, st));
+      TBK_CUDA(cudaMemsetAsync(Rs.as<char>() + kt0 * tile, 0, (size_t)(kt1 - kt0) * tile, st));
+    }
+  }
   TBK_CUDA(cudaMemsetAsync(work.p, 0, work.bytes, st));
   TBK_TRY(macc.alloc(sizeof(double2) * (size_t)M * M));
   TBK_CUDA(cudaMemsetAsync(macc.p, 0, macc.bytes, st));
@@ -376,6 +467,7 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
       for (tbk_sparse_s* o : {AL, AR}) if (o) TBK_TRY(ensure_ell_dd(o, st));
   }
   TBK_TRY(partd.alloc(sizeof(double) * 2 * gmax));
+  trace.mark("alloc+classes");
   char* wb = work.as<char>();
   auto wblk = [&](int i) { return static_cast<void*>(wb + (size_t)i * blk * csz); };
   void* v0 = wblk(5);
@@ -560,6 +652,7 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
       TBK_TRY(side(AR, BR, Rs.as<float2>()));
     }
     TBK_CUDA(cudaEventRecord(ev[1], st));
+    trace.mark("blocks");
     if (f64b) {
       dim3 g((M + kGT - 1) / kGT, (M + kGT - 1) / kGT, nsplit);
       mu_gemm_f64_kernel<<<g, 256, 0, st>>>(Ls.as<double2>(), Rs.as<double2>(), M, blk, ksplit, part.as<double2>());
@@ -579,6 +672,7 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
     }
     TBK_CUDA(cudaEventRecord(ev[2], st));
     TBK_CUDA(cudaEventSynchronize(ev[2]));
+    trace.mark("gemm");
     float a = 0.f, b = 0.f;
     TBK_CUDA(cudaEventElapsedTime(&a, ev[0], ev[1]));
     TBK_CUDA(cudaEventElapsedTime(&b, ev[1], ev[2]));
@@ -603,6 +697,15 @@ int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_
   TBK_CHECK_LAUNCH();
   TBK_CUDA(cudaMemcpyAsync(mu_out, macc.p, sizeof(double2) * (size_t)M * M, cudaMemcpyDeviceToHost, st));
   TBK_CUDA(cudaStreamSynchronize(st));
+  trace.mark("scale+readback");
+  Ls.release();
+  Rs.release();
+  work.release();
+  if (kctx.pool) {
+    TBK_CUDA(cudaStreamSynchronize(st));
+    TBK_CUDA(cudaMemPoolTrimTo(kctx.pool, kKuboPoolKeep));   // keep at most kKuboPoolKeep bytes
+  }
+  trace.mark("free");
   return TBK_OK;
 }
 
