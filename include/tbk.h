@@ -395,10 +395,16 @@ enum {
  * free device memory).
  * kets: host N x R column-major complex128, or NULL for seeded random phases.
  * kernel: TBK_KERNEL_* with parameters kp0/kp1 (g_m).  flags: TBK_MU_*.
- * mu_out: host M x M complex128, row m = left index. */
+ * mu_out: host M x M complex128, row m = left index.
+ * Stores and work blocks of at most 16 GB come from a per-device pool that
+ * keeps them for the next call (tbk_kubo_release returns them); larger ones
+ * are allocated and freed in the call. */
 int tbk_kubo_mu(tbk_sparse Ht, tbk_sparse AL, tbk_sparse BL, tbk_sparse AR, tbk_sparse BR, int32_t M,
                 int32_t R, uint64_t seed, const double* kets, int32_t kernel_kind, double kp0,
                 double kp1, int32_t flags, double block_budget_gb, double* mu_out, void* stream);
+/* Returns the memory tbk_kubo_mu's pool keeps on the current device (no
+ * counterpart in the reference).  Calls in flight keep theirs. */
+int tbk_kubo_release(void);
 /* Device time of the last tbk_kubo_mu call in this process (CUDA events on its
  * stream): building the stored blocks, the mu GEMM (+ split-K reduction), the
  * real flops of the GEMM products issued (3 split-TF32 terms on the tensor

@@ -244,3 +244,20 @@ def test_greenwood_mu_fcc_wide_rows(gpu):
     assert _rel(mu, ref) <= MU_TOL, _rel(mu, ref)
     assert np.array_equal(mu, tb.kubo_mu(Ht, v_x, v_x, None, None, fuse_ops=True, **kw))
     assert np.array_equal(mu, tb.kubo_mu(Ht, v_x, v_x, None, None, fuse_ops=True, both_sides=True, **kw))
+
+
+def test_repeated_calls_reuse_pool_and_release(gpu):
+    """Stores of at most 16 GB come from a pool kept between calls: repeated
+    calls give the same bits, and so does a call after tbk_kubo_release."""
+    tb = gpu
+    X, H = _system(tb, L=(20, 18))
+    Ht = tb.GreenFunction(48, H, -4.1, 4.1).scaled_HE
+    v_x = tb.commutator(Ht, X.op_position(0))
+    v_y = tb.commutator(Ht, X.op_position(1))
+    kw = dict(M=48, R=5, seed=3, kernel=tb.Lorentz(6.0), tensor=True)
+    a = tb.kubo_mu(Ht, None, None, v_x, v_y, **kw)
+    b = tb.kubo_mu(Ht, None, None, v_x, v_y, **kw)
+    assert np.array_equal(a, b)
+    tb.kubo_release()
+    tb.kubo_release()                                   # twice: nothing left to return
+    assert np.array_equal(tb.kubo_mu(Ht, None, None, v_x, v_y, **kw), a)

@@ -8,7 +8,7 @@ from .capi import TbkError, device_count
 from .lattice import (Chain, Cubic, FCC, Honeycomb, Kagome, Lieb, PartialLattice, SparseMatrix, Square, TI_sp,
                       UnitCell, commutator, graphene, sawtooth_chain_p, sawtooth_chain_X, stub_1d_p, stub_1d_X)
 from .kubo import (bastin_integrate, bastin_zeta, chebyshev_nodes, conductivity_Kubo_Bastin, conductivity_spectrum,
-                   generate_V_moments, greenwood_sigma, kubo_last_timing, kubo_mu, mu_from_blocks,
+                   generate_V_moments, greenwood_sigma, kubo_last_timing, kubo_mu, kubo_release, mu_from_blocks,
                    conductivity_test_sawtooth)
 from .kpm import (Cheb_first_kind_seq_braket, Dirichlet, Fejer, GreenFunction, GreenFunctionImag, Jackson,
                   KpmSolver, Kernel, Lanczos, Lorentz, Wang_and_Zunger, bases_of_uniform_ampl_with_random_phases,

@@ -135,6 +135,7 @@ SIGNATURES = {
     "tbk_cheb_braket_real": (C.c_int, [_i32, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _i32, _i32, _vp]),
     "tbk_cheb_braket_complex": (C.c_int, [_i32, _i64, _vp, _vp, _vp, _i32, _vp, _vp, _i32, _i32, _vp]),
     "tbk_cheb_braket_release": (None, []),
+    "tbk_kubo_release": (C.c_int, []),
     "tbk_set_wait_limit": (C.c_int, [_i64]),
     "tbk_kpm_create": (C.c_int, [C.POINTER(_vp), _vp, _i32, _i32]),
     "tbk_kpm_run": (C.c_int, [_vp, _i32, _vp, _vp, _vp, _vp]),

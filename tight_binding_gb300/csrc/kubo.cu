@@ -766,6 +766,14 @@ int tbk_mu_from_blocks(int32_t M, int64_t K, const double* L, const double* Rb, 
   return TBK_OK;
 }
 
+int tbk_kubo_release(void) {
+  cudaMemPool_t pl = kubo_pool();
+  if (!pl) return TBK_OK;
+  TBK_CUDA(cudaDeviceSynchronize());
+  TBK_CUDA(cudaMemPoolTrimTo(pl, 0));
+  return TBK_OK;
+}
+
 int tbk_kubo_last_timing(double* ms_blocks, double* ms_gemm, double* gemm_flops, double* block_bytes, int32_t* chunks) {
   KuboTiming t;
   {

@@ -57,6 +57,12 @@ def kubo_mu(Ht: SparseMatrix, AL=None, BL=None, AR=None, BR=None, M: int = 64, R
     return mu
 
 
+def kubo_release() -> None:
+    """Return the device memory kubo_mu's pool keeps between calls (stores and
+    work blocks of at most 16 GB)."""
+    check(lib().tbk_kubo_release())
+
+
 def mu_from_blocks(L: np.ndarray, R: np.ndarray, tensor: bool = True) -> np.ndarray:
     """mu_mn = sum_k conj(L[m, k]) R[n, k] on the GPU (blocks rounded to complex64)."""
     L = np.ascontiguousarray(L, dtype=np.complex128)
