@@ -59,6 +59,9 @@ struct SLane {                      // up to 64 vectors of one request (device v
   void* va;                         // v_s for even s
   void* vb;                         // v_s for odd s
   int32_t n, n_steps, s0, req;
+  // the lane's slab partials are part[slab_begin ..+ n_slabs): kSrvWarps per
+  // tile (its first tile is slab_begin / kSrvWarps), the last tile's slabs
+  // past the rows hold zeros; slab_rows rows per slab
   int32_t slab_begin, n_slabs, slab_rows, cls_w;   // cls_w: class form, entries per class
   int32_t n_cls, pad;               // class form: classes
 };
@@ -71,7 +74,7 @@ struct SReq {
   int32_t lane0, n_lanes, s0, n_steps, n_mom, finishing;
 };
 struct SHdr {
-  int32_t grp_begin[kGroups];
+  int32_t grp_begin[kGroups];       // a group's tiles: tiles[grp_begin .. + grp_count)
   int32_t grp_count[kGroups];
   int32_t n_lanes, n_tiles, n_reqs, pad;
 };
