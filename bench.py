@@ -21,7 +21,8 @@ SpMM + cuBLAS dot per moment, restated in baseline/cusparse_kpm.cu), the CPU
 oracle (the reference's CPU recursion restated in C, OpenMP over the random
 vectors) on a bounded sample, full-size parity (all moments and rho against
 the complex128 recursion), and one sub-record per other configuration
-(`configs`: 1, 3, 5 and a shortened 4).
+(`configs`: 1, 3, 5 and a shortened 4; configs 3 and 5 with the reference's
+CPU Kubo path timed on bounded samples and extrapolated to one solve).
 
 --impl reference: times the CPU restatement of the reference's KPM loop
 (TB/numerical.h:363-381) on all host cores, on a bounded sample of the same
