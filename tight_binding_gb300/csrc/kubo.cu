@@ -318,7 +318,8 @@ struct PhaseTrace {
 // The stored blocks and work blocks of a call made outside a server come
 // from a stream-ordered pool that keeps up to kKuboPoolKeep bytes between
 // calls: stores of that size are then reused instead of mapped and unmapped
-// every call (config 3: 8.6 GB, whose cudaFree took 5.7 ms of a 36 ms call).
+// every call (the 256 x 256, M = 512, R = 16 Bastin case: 8.6 GB, whose
+// cudaFree took 5.7 ms of a 36 ms call).
 // Larger stores keep plain allocations (a 137 GB store from the pool, then
 // trimmed, measured 0.2 s slower than cudaMalloc and cudaFree); each call
 // trims the pool back to kKuboPoolKeep before it returns.
