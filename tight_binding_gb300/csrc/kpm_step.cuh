@@ -128,6 +128,20 @@ __global__ void __launch_bounds__(kStepThreads) kpm_step_kernel(
             if (!FIRST) bulk_prefetch_l2(pv + rf * R, vb);
             if (BRAKET) bulk_prefetch_l2(bras + rf * R, vb);
           }
+          if constexpr (!CLS) {
+            if (gather) {
+              // and the ELL columns and values of its slices, so that the rows'
+              // column loads find them in L2 (slice offsets are whole 32-entry
+              // columns: 128-byte aligned, whole 128-byte multiples)
+              constexpr uint32_t VB = (CPLX_H ? 2u : 1u) * (uint32_t)sizeof(F);
+              const int32_t s0 = (int32_t)(rf >> 5), s1 = (int32_t)((rf + nr - 1) >> 5);
+              const int32_t o0 = soff[s0], o1 = soff[s1 + 1];
+              if (o1 > o0) {
+                bulk_prefetch_l2(ecol + o0, (uint32_t)(o1 - o0) * 4u);
+                bulk_prefetch_l2(reinterpret_cast<const char*>(eval) + (int64_t)o0 * VB, (uint32_t)(o1 - o0) * VB);
+              }
+            }
+          }
         }
       }
     }
