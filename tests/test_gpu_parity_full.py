@@ -9,7 +9,7 @@ The complex64 recursion is compared over all 2048 moments with the complex128
 (FP64) recursion of the same seeded vectors — the plain path that the smaller
 tests pin to the CPU oracle at 1e-10 — and with the double-float recursion.
 
-Stated bounds (spec target: DoS within 1e-5 relative of the FP64 run):
+Stated bounds (the target: DoS within 1e-5 relative of the FP64 run):
   max_n |mu_n(mixed) - mu_n(fp64)| / mu_0            <= MU_TOL
   max_E |rho_mixed(E) - rho_fp64(E)| / max_E rho_fp64 <= RHO_TOL
   max_n |mu_n(dd) - mu_n(fp64)| / mu_0               <= 1e-10
